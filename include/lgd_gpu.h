@@ -1,0 +1,183 @@
+/*
+ * lgd_gpu.h - C ABI of the GB300 (sm_103a) cell-update library.
+ *
+ * This is the drop-in boundary for LibGeoDecomp's CUDASimulator<CELL> hot
+ * path: plain C types, pointers and sizes only.  Every entry point returns
+ * an int status (LGD_OK = 0); on failure lgd_gpu_last_error() gives the
+ * message.  No C++ exception crosses this boundary; the C++ host layer
+ * (libgeodecomp_gb300/include/libgeodecomp_gb300/gb300simulator.h) turns
+ * non-zero codes back into the exceptions the reference throws.
+ *
+ * Threading: one host thread per handle (the reference's CUDASimulator has
+ * no locking either).  All work of a handle runs on that handle's CUDA
+ * stream; calls that return data to the host synchronise that stream.
+ *
+ * Grid layout in host buffers: dense, x-fastest, idx = (z*ny + y)*nx + x,
+ * one array per cell member (structure of arrays, the layout libflatarray
+ * gives SoA cells, lib/libflatarray/include/libflatarray/detail/macros.hpp:
+ * 99-106, minus its size buckets and padding).
+ */
+#ifndef LGD_GPU_H
+#define LGD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes
+ * Reference counterparts: LGD_ERR_INVALID ~ std::invalid_argument /
+ * std::logic_error (storage/*.h), LGD_ERR_RANGE ~ std::out_of_range thrown by
+ * the size-bucket dispatch (lib/libflatarray/include/libflatarray/macros.hpp:
+ * 948-1060), LGD_ERR_CUDA ~ std::runtime_error("CUDA error") from
+ * CUDAUtil::checkForError (misc/cudautil.h:48-55). */
+#define LGD_OK 0
+#define LGD_ERR_INVALID 1
+#define LGD_ERR_RANGE 2
+#define LGD_ERR_CUDA 3
+#define LGD_ERR_NOMEM 4
+#define LGD_ERR_TIMEOUT 5
+#define LGD_ERR_UNSUPPORTED 6
+
+/* Copies the last error message of the calling thread into buf (always
+ * NUL-terminated when len > 0); returns the last status code. */
+int lgd_gpu_last_error(char *buf, size_t len);
+
+/* Library version as 10000*major + 100*minor + patch. */
+int lgd_gpu_version(void);
+
+/* Number of CUDA devices visible (0 on a machine without a GPU). */
+int lgd_gpu_device_count(int *count);
+
+/* ------------------------------------------------------ structured grids
+ * Cell kinds compiled into the library.  Each one is the device-side
+ * restatement of a Cell class's update()/updateLineX(); the member list is
+ * the cell's SoA registration in declaration order.
+ *   LGD_CELL_JACOBI7_F64   members {double temp}; von Neumann r=1, 3D;
+ *                          temp' = (c+n+s+e+w+t+b) * (1/7) (IEEE FP64,
+ *                          bit-identical to the reference's SerialSimulator)
+ *   LGD_CELL_JACOBI7_F64_FIX same cell with FP64 values at the ABI; on the
+ *                          device the grid is held in 64-bit fixed point,
+ *                          value = k * 2^(e - 60) with e the smallest power
+ *                          of two above every value uploaded so far and the
+ *                          edge cell.  The neighbour sum is exact and the
+ *                          division by 7 rounds to the nearest unit, so each
+ *                          step adds at most 2^(e - 61) absolute error.  For
+ *                          GPUs whose FP64 pipe, not memory, would bound the
+ *                          IEEE kernel.
+ *   LGD_CELL_JACOBI7_F32   members {float temp}; same stencil in FP32
+ *   LGD_CELL_SUM6_F64      members {double valA, double valB}; valB' = the
+ *                          six face neighbours' valA summed in the order
+ *                          (0,0,-1) (0,-1,0) (-1,0,0) (1,0,0) (0,1,0) (0,0,1)
+ *                          (storage/test/unit/fixedneighborhoodupdatefunctortest.h:
+ *                          30-46); valA' = valA
+ *   LGD_CELL_GOL_U8        members {uint8 alive}; Moore r=1, 2D; Conway's rule
+ *                          (src/examples/gameoflife/main.cpp:35-58)
+ *   LGD_CELL_VARCOEF_F32 / _F64  members {u, k}; von Neumann r=1, 3D;
+ *                          u' = u + sum_faces 0.5 (k + k_nb)(u_nb - u), faces
+ *                          -x,+x,-y,+y,-z,+z; k' = k
+ */
+#define LGD_CELL_JACOBI7_F64 1
+#define LGD_CELL_JACOBI7_F64_FIX 2
+#define LGD_CELL_JACOBI7_F32 3
+#define LGD_CELL_SUM6_F64 4
+#define LGD_CELL_GOL_U8 5
+#define LGD_CELL_VARCOEF_F32 6
+#define LGD_CELL_VARCOEF_F64 7
+
+/* periodic bit d set: axis d (0 = x, 1 = y, 2 = z) wraps (Topologies::Torus);
+ * clear: cells outside read the constant edge cell (Topologies::Cube with
+ * SoAGrid's edge cell, storage/soagrid.h:578-585, geometry/topologies.h:
+ * 263-278). */
+typedef struct lgd_grid_desc {
+    int dim;            /* 2 or 3 */
+    int nx, ny, nz;     /* cells per axis; nz = 1 for 2D */
+    int periodic;       /* bit mask, see above */
+    int cell;           /* LGD_CELL_* */
+    int flags;          /* reserved, 0 */
+    double edge[4];     /* edge cell, one value per member */
+} lgd_grid_desc;
+
+typedef struct lgd_handle lgd_handle;
+
+/* Allocates the double-buffered device grid.  Replaces the device part of
+ * CUDASimulator's constructor (parallelization/cudasimulator.h:314-429:
+ * cudaMalloc of the old/new grids, offsets, wrap setup).  Sizes up to
+ * 2^31-1 cells per axis; the reference's SoA size buckets stop at 1032
+ * per 3D axis (lib/libflatarray/include/libflatarray/api_traits.hpp:120-123)
+ * and this library has no such limit. */
+int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out);
+int lgd_gpu_destroy(lgd_handle *h);
+
+/* Host <-> device copy of one member of one buffer (which: 0 = current
+ * grid, 1 = next grid); bytes must equal nx*ny*nz*sizeof(member).  Replaces
+ * the H2D copies of CUDASimulator::run (parallelization/cudasimulator.h:
+ * 515-516) and the D2H copy of getGrid (:490-497).  Downloads synchronise. */
+int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_t bytes);
+int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t bytes);
+
+/* Streak-wise copies for plugins that need part of the grid (reference:
+ * GridBase::saveRegion / loadRegion, storage/gridbase.h; the libflatarray
+ * streak functors save_functor.hpp / load_functor.hpp).  streaks holds
+ * n_streaks * 4 ints (x, y, z, endX); the buffer packs the streaks' cells in
+ * order. */
+int lgd_gpu_save_region(lgd_handle *h, int member, const int *streaks, int n_streaks, void *host, size_t bytes);
+int lgd_gpu_load_region(lgd_handle *h, int member, const int *streaks, int n_streaks, const void *host, size_t bytes);
+
+/* Advances the whole grid count time steps (current -> next, then swap),
+ * starting at nano step nano_step.  Replaces CUDASimulator::step's nanoStep
+ * loop with its pointer swap (parallelization/cudasimulator.h:467-470) and
+ * the kernel2D/kernel3D launch (:566-590).  Asynchronous on the handle's
+ * stream. */
+int lgd_gpu_step(lgd_handle *h, unsigned nano_step, int count);
+
+/* Updates only the cells of the streaks (n_streaks * 4 ints: x, y, z,
+ * endX) from the current grid into the next grid; no swap.  Replaces
+ * UpdateFunctor<CELL>()(region, ..., gridOld, &gridNew, nanoStep)
+ * (storage/updatefunctor.h:403-428). */
+int lgd_gpu_update_region(lgd_handle *h, const int *streaks, int n_streaks, unsigned nano_step);
+
+/* Swaps current and next (the simulator's std::swap of grid pointers,
+ * parallelization/serialsimulator.h:137-138). */
+int lgd_gpu_swap(lgd_handle *h);
+
+/* Fills one member of one buffer with the library's seeded uniform [0,1)
+ * doubles (SplitMix64, value i = top 53 bits of mix(key + (i+1)*GAMMA),
+ * key = mix(seed*256 + stream)); FP32 members get the double rounded.
+ * Test and benchmark helper: lets large grids be initialised on device. */
+int lgd_gpu_fill_uniform(lgd_handle *h, int member, int which, uint64_t seed, int stream);
+
+/* Bernoulli(p) 0/1 fill of a uint8 member from the same stream
+ * (value i = 1 if uniform_i < p). */
+int lgd_gpu_fill_bernoulli(lgd_handle *h, int member, int which, uint64_t seed, int stream, double p);
+
+/* Fixed-point exponent e of an LGD_CELL_JACOBI7_F64_FIX grid. */
+int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or
+ * order their own work against the library's. */
+int lgd_gpu_stream(lgd_handle *h, void **stream);
+
+/* Sum of one member over the whole grid in FP64 (deterministic order). */
+int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum);
+
+int lgd_gpu_synchronize(lgd_handle *h);
+
+/* Device pointer and row pitch (bytes) of one member of one buffer; the
+ * grid is pitched: row (y, z) starts at ptr + ((z*ny + y) * pitch). */
+int lgd_gpu_device_ptr(lgd_handle *h, int member, int which, void **ptr, size_t *pitch_bytes);
+
+/* Number of kernel launches this handle has issued (for benchmarking). */
+int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count);
+
+/* Temporal blocking depth used by lgd_gpu_step where the cell supports it
+ * (time steps fused per pass over memory); 0 = library default. */
+int lgd_gpu_set_time_block(lgd_handle *h, int depth);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

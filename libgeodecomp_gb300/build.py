@@ -1,0 +1,63 @@
+"""Build the library in-tree: nvcc for sm_103a, one object per source,
+compiled in parallel, linked into libgeodecomp_gb300/liblgd_gb300.so."""
+from __future__ import annotations
+
+import concurrent.futures
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "liblgd_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _compile(src: str, verbose_ptxas: bool) -> str:
+    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+    deps = [src] + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
+        [os.path.join(os.path.dirname(HERE), "include", "lgd_gpu.h")]
+    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
+        return obj
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+           "-I", os.path.join(os.path.dirname(HERE), "include"), "-c", src, "-o", obj + ".tmp"]
+    if src.endswith(".cpp"):
+        cmd = [nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+               "-I", os.path.join(os.path.dirname(HERE), "include"), "-x", "c++", "-c", src, "-o", obj + ".tmp"]
+    if verbose_ptxas and src.endswith(".cu"):
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("compile failed: %s\n%s\n%s" % (" ".join(cmd), res.stdout, res.stderr))
+    if verbose_ptxas:
+        sys.stderr.write(res.stderr)
+    os.replace(obj + ".tmp", obj)
+    return obj
+
+
+def build(verbose_ptxas: bool = False) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(16, len(sources))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), sources))
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", LIB + ".tmp", *objs]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s" % (res.stdout, res.stderr))
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose_ptxas="-v" in sys.argv))

@@ -1,0 +1,593 @@
+// C ABI of the structured-grid part: handle lifetime, host <-> device
+// copies, stepping, region updates.  See include/lgd_gpu.h for the
+// contract and the reference entry points each function replaces.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lgd_internal.h"
+#include "k_common.cuh"
+
+namespace lgd {
+
+static thread_local int t_last_code = LGD_OK;
+static thread_local std::string t_last_msg;
+
+void set_error(int code, const std::string& msg)
+{
+    t_last_code = code;
+    t_last_msg = msg;
+}
+
+void clear_error()
+{
+    t_last_code = LGD_OK;
+    t_last_msg.clear();
+}
+
+struct CellInfo {
+    int n_members;
+    int elem[2];        // device element size per member
+    int host_elem[2];   // element size at the ABI
+    bool is_static[2];
+    int dim_min, dim_max;
+};
+
+static CellInfo cell_info(int cell)
+{
+    switch (cell) {
+    case LGD_CELL_JACOBI7_F64:     return {1, {8, 0}, {8, 0}, {false, false}, 3, 3};
+    case LGD_CELL_JACOBI7_F64_FIX: return {1, {8, 0}, {8, 0}, {false, false}, 3, 3};
+    case LGD_CELL_JACOBI7_F32:     return {1, {4, 0}, {4, 0}, {false, false}, 3, 3};
+    case LGD_CELL_SUM6_F64:        return {2, {8, 8}, {8, 8}, {false, false}, 3, 3};
+    case LGD_CELL_GOL_U8:          return {1, {1, 0}, {1, 0}, {false, false}, 2, 2};
+    case LGD_CELL_VARCOEF_F32:     return {2, {4, 4}, {4, 4}, {false, true}, 3, 3};
+    case LGD_CELL_VARCOEF_F64:     return {2, {8, 8}, {8, 8}, {false, true}, 3, 3};
+    default:
+        throw Error(LGD_ERR_INVALID, "unknown cell kind " + std::to_string(cell));
+    }
+}
+
+// ---------------------------------------------------------- fixed point
+// The FP64 Jacobi grid in fixed-point form: value = k * 2^(fix_exp - 60).
+// fix_exp is chosen at upload so that every value and the edge cell fit
+// (|value| <= 2^fix_exp); averaging never leaves that range.
+static int exp_bound(double m)
+{
+    if (!(m > 0.0)) return 0;
+    int e = 0;
+    double f = std::frexp(m, &e);   // m = f * 2^e, f in [0.5, 1)
+    (void)f;
+    return e;                        // 2^e > m
+}
+
+long long fix_edge(const Grid& g)
+{
+    return std::llrint(std::ldexp(g.desc.edge[0], 60 - g.fix_exp));
+}
+
+int fix_scale_exp(const Grid& g)
+{
+    return g.fix_exp;
+}
+
+// dense (x-fastest, rows of nx) doubles -> pitched fixed point
+__global__ void to_fix_pitched_kernel(const double *src, long long *dst, int nx, long long rows, long long pitch, int exp)
+{
+    const long long n = (long long)nx * rows;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / nx;
+        const long long x = i - r * nx;
+        dst[r * pitch + x] = __double2ll_rn(ldexp(src[i], 60 - exp));
+    }
+}
+
+__global__ void from_fix_pitched_kernel(const long long *src, double *dst, int nx, long long rows, long long pitch, int exp)
+{
+    const long long n = (long long)nx * rows;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / nx;
+        const long long x = i - r * nx;
+        dst[i] = ldexp((double)src[r * pitch + x], exp - 60);
+    }
+}
+
+// per-block max |v| (NaN propagates as NaN through fmax's operand order
+// being irrelevant: a NaN block result is turned into +inf so the host sees
+// a non-finite maximum)
+__global__ void absmax_kernel(const double *v, long long n, double *partial)
+{
+    __shared__ double red[256];
+    double m = 0.0;
+    bool bad = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double a = fabs(v[i]);
+        bad |= !(a <= 1.7976931348623157e308);
+        m = fmax(m, a);
+    }
+    red[threadIdx.x] = bad ? __longlong_as_double(0x7ff0000000000000ll) : m;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void rescale_fix_kernel(long long *buf, long long n, int shift)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long v = buf[i];
+        buf[i] = (v + (1ll << (shift - 1))) >> shift;
+    }
+}
+
+static size_t buffer_elems(const Grid& g, int member)
+{
+    return g.pitch_bytes[member] / g.m[member].elem * (size_t)g.desc.ny * g.desc.nz;
+}
+
+// Raises fix_exp to at least e, rescaling both buffers.
+static void raise_fix_exp(Grid& g, int e)
+{
+    if (e <= g.fix_exp) return;
+    const int shift = e - g.fix_exp;
+    const long long n = (long long)buffer_elems(g, 0);
+    for (int b = 0; b < 2; ++b) {
+        if (shift >= 62) {
+            LGD_CHECK_CUDA(cudaMemsetAsync(g.m[0].buf[b], 0, n * 8, g.stream));
+        } else {
+            rescale_fix_kernel<<<152 * 4, 256, 0, g.stream>>>((long long *)g.m[0].buf[b], n, shift);
+            check_launch("rescale");
+            ++g.launches;
+        }
+    }
+    g.fix_exp = e;
+}
+
+// --------------------------------------------------------------- helpers
+static Grid& grid_of(lgd_handle *h)
+{
+    LGD_REQUIRE(h != nullptr, LGD_ERR_INVALID, "null handle");
+    return h->g;
+}
+
+static void check_member(const Grid& g, int member, int which)
+{
+    LGD_REQUIRE(member >= 0 && member < g.n_members, LGD_ERR_INVALID, "member index out of range");
+    LGD_REQUIRE(which == 0 || which == 1, LGD_ERR_INVALID, "which must be 0 (current) or 1 (next)");
+}
+
+static void *member_buf(Grid& g, int member, int which)
+{
+    if (g.m[member].is_static) return g.m[member].buf[0];
+    return g.m[member].buf[which ? 1 - g.cur : g.cur];
+}
+
+static size_t cells_of(const Grid& g)
+{
+    return (size_t)g.desc.nx * g.desc.ny * g.desc.nz;
+}
+
+// Validates streaks (x, y, z, endX) and stages them plus their prefix sums
+// on the device; returns the number of cells.
+static long long stage_streaks(Grid& g, const int *streaks, int n)
+{
+    LGD_REQUIRE(n >= 0, LGD_ERR_INVALID, "negative streak count");
+    LGD_REQUIRE(n == 0 || streaks != nullptr, LGD_ERR_INVALID, "null streak list");
+    std::vector<long long> prefix(n > 0 ? n : 1);
+    long long total = 0;
+    for (int i = 0; i < n; ++i) {
+        const int x = streaks[4 * i];
+        const int y = streaks[4 * i + 1];
+        const int z = streaks[4 * i + 2];
+        const int end = streaks[4 * i + 3];
+        LGD_REQUIRE(x >= 0 && end <= g.desc.nx && x <= end, LGD_ERR_RANGE, "streak outside the grid in x");
+        LGD_REQUIRE(y >= 0 && y < g.desc.ny, LGD_ERR_RANGE, "streak outside the grid in y");
+        LGD_REQUIRE(z >= 0 && z < g.desc.nz, LGD_ERR_RANGE, "streak outside the grid in z");
+        prefix[i] = total;
+        total += end - x;
+    }
+    if (n > g.streak_capacity) {
+        if (g.d_streaks) cudaFree(g.d_streaks);
+        if (g.d_streak_prefix) cudaFree(g.d_streak_prefix);
+        g.d_streaks = nullptr;
+        g.d_streak_prefix = nullptr;
+        g.streak_capacity = 0;
+        LGD_CHECK_CUDA(cudaMalloc(&g.d_streaks, sizeof(int) * 4 * n));
+        LGD_CHECK_CUDA(cudaMalloc(&g.d_streak_prefix, sizeof(long long) * n));
+        g.streak_capacity = n;
+    }
+    if (n > 0) {
+        LGD_CHECK_CUDA(cudaMemcpyAsync(g.d_streaks, streaks, sizeof(int) * 4 * n, cudaMemcpyHostToDevice, g.stream));
+        LGD_CHECK_CUDA(cudaMemcpyAsync(g.d_streak_prefix, prefix.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, g.stream));
+        // the staging arrays are host stack/heap memory: finish before they go
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    }
+    return total;
+}
+
+void launch_fill(Grid& g, int member, int which, uint64_t seed, int stream, int mode, double p, int scale_exp);
+
+}  // namespace lgd
+
+using namespace lgd;
+
+extern "C" {
+
+int lgd_gpu_last_error(char *buf, size_t len)
+{
+    if (buf && len > 0) {
+        std::strncpy(buf, t_last_msg.c_str(), len - 1);
+        buf[len - 1] = '\0';
+    }
+    return t_last_code;
+}
+
+int lgd_gpu_version(void)
+{
+    return 10000;
+}
+
+int lgd_gpu_device_count(int *count)
+{
+    return guard([&] {
+        LGD_REQUIRE(count != nullptr, LGD_ERR_INVALID, "null count");
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        *count = n;
+    });
+}
+
+int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
+{
+    return guard([&] {
+        LGD_REQUIRE(desc != nullptr && out != nullptr, LGD_ERR_INVALID, "null argument");
+        *out = nullptr;
+        const CellInfo ci = cell_info(desc->cell);
+        LGD_REQUIRE(desc->dim >= ci.dim_min && desc->dim <= ci.dim_max, LGD_ERR_INVALID, "dimension does not match the cell");
+        LGD_REQUIRE(desc->nx > 0 && desc->ny > 0 && desc->nz > 0, LGD_ERR_INVALID, "grid dimensions must be positive");
+        LGD_REQUIRE(desc->dim == 3 || desc->nz == 1, LGD_ERR_INVALID, "2D grids have nz = 1");
+        LGD_REQUIRE((desc->periodic & ~7) == 0, LGD_ERR_INVALID, "periodic mask has bits beyond z");
+        int ndev = 0;
+        LGD_CHECK_CUDA(cudaGetDeviceCount(&ndev));
+        LGD_REQUIRE(ndev > 0, LGD_ERR_CUDA, "no CUDA device");
+
+        lgd_handle *h = new lgd_handle();
+        Grid& g = h->g;
+        std::memset(&g, 0, sizeof(Grid));
+        g.desc = *desc;
+        g.n_members = ci.n_members;
+        LGD_CHECK_CUDA(cudaGetDevice(&g.device));
+        try {
+            LGD_CHECK_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+            for (int m = 0; m < ci.n_members; ++m) {
+                g.m[m].elem = ci.elem[m];
+                g.m[m].is_static = ci.is_static[m];
+                g.pitch_bytes[m] = (size_t)round_up(desc->nx * ci.elem[m], 128);
+                const size_t bytes = g.pitch_bytes[m] * (size_t)desc->ny * desc->nz;
+                for (int b = 0; b < (ci.is_static[m] ? 1 : 2); ++b) {
+                    LGD_CHECK_CUDA(cudaMalloc(&g.m[m].buf[b], bytes));
+                    LGD_CHECK_CUDA(cudaMemsetAsync(g.m[m].buf[b], 0, bytes, g.stream));
+                }
+            }
+            g.pitch_elems = g.pitch_bytes[0] / ci.elem[0];
+            g.plane_elems = g.pitch_elems * desc->ny;
+            if (desc->cell == LGD_CELL_JACOBI7_F64_FIX) {
+                g.fix_exp = exp_bound(std::fabs(desc->edge[0]));
+            }
+            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+        } catch (...) {
+            for (int m = 0; m < 2; ++m) {
+                for (int b = 0; b < 2; ++b) {
+                    if (g.m[m].buf[b]) cudaFree(g.m[m].buf[b]);
+                }
+            }
+            if (g.stream) cudaStreamDestroy(g.stream);
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int lgd_gpu_destroy(lgd_handle *h)
+{
+    return guard([&] {
+        if (!h) return;
+        Grid& g = h->g;
+        cudaStreamSynchronize(g.stream);
+        for (int m = 0; m < 2; ++m) {
+            for (int b = 0; b < 2; ++b) {
+                if (g.m[m].buf[b]) cudaFree(g.m[m].buf[b]);
+            }
+        }
+        if (g.d_streaks) cudaFree(g.d_streaks);
+        if (g.d_streak_prefix) cudaFree(g.d_streak_prefix);
+        if (g.d_partials) cudaFree(g.d_partials);
+        cudaStreamDestroy(g.stream);
+        delete h;
+    });
+}
+
+int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_t bytes)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        const size_t n = cells_of(g);
+        const int helem = g.m[member].elem;
+        LGD_REQUIRE(host != nullptr, LGD_ERR_INVALID, "null host buffer");
+        LGD_REQUIRE(bytes == n * helem, LGD_ERR_INVALID, "byte count does not match the grid");
+        const size_t rows = (size_t)g.desc.ny * g.desc.nz;
+        if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
+            // stage the doubles on the device, find max |value| there, then
+            // convert into the pitched fixed-point buffer
+            double *tmp = nullptr;
+            LGD_CHECK_CUDA(cudaMallocAsync(&tmp, n * 8 + 8 * 1024, g.stream));
+            double *partial = tmp + n;
+            LGD_CHECK_CUDA(cudaMemcpyAsync(tmp, host, n * 8, cudaMemcpyHostToDevice, g.stream));
+            absmax_kernel<<<1024, 256, 0, g.stream>>>(tmp, (long long)n, partial);
+            check_launch("max |value|");
+            ++g.launches;
+            double hpart[1024];
+            LGD_CHECK_CUDA(cudaMemcpyAsync(hpart, partial, sizeof(hpart), cudaMemcpyDeviceToHost, g.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            double m = std::fabs(g.desc.edge[0]);
+            for (int i = 0; i < 1024; ++i) m = std::fmax(m, hpart[i]);
+            if (!std::isfinite(m)) {
+                cudaFreeAsync(tmp, g.stream);
+                cudaStreamSynchronize(g.stream);
+                throw Error(LGD_ERR_INVALID, "grid holds a non-finite value");
+            }
+            raise_fix_exp(g, exp_bound(m));
+            long long *dst = (long long *)member_buf(g, member, which);
+            const size_t pitch = g.pitch_bytes[0] / 8;
+            to_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(tmp, dst, g.desc.nx, (long long)rows, (long long)pitch, g.fix_exp);
+            check_launch("to fixed point");
+            ++g.launches;
+            LGD_CHECK_CUDA(cudaFreeAsync(tmp, g.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            return;
+        }
+        LGD_CHECK_CUDA(cudaMemcpy2DAsync(member_buf(g, member, which), g.pitch_bytes[member], host,
+                                         (size_t)g.desc.nx * helem, (size_t)g.desc.nx * helem, rows,
+                                         cudaMemcpyHostToDevice, g.stream));
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t bytes)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        const size_t n = cells_of(g);
+        const int helem = g.m[member].elem;
+        LGD_REQUIRE(host != nullptr, LGD_ERR_INVALID, "null host buffer");
+        LGD_REQUIRE(bytes == n * helem, LGD_ERR_INVALID, "byte count does not match the grid");
+        const size_t rows = (size_t)g.desc.ny * g.desc.nz;
+        if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
+            double *tmp = nullptr;
+            LGD_CHECK_CUDA(cudaMallocAsync(&tmp, n * 8, g.stream));
+            const long long *src = (const long long *)member_buf(g, member, which);
+            const size_t pitch = g.pitch_bytes[0] / 8;
+            from_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(src, tmp, g.desc.nx, (long long)rows, (long long)pitch, g.fix_exp);
+            check_launch("from fixed point");
+            ++g.launches;
+            LGD_CHECK_CUDA(cudaMemcpyAsync(host, tmp, n * 8, cudaMemcpyDeviceToHost, g.stream));
+            LGD_CHECK_CUDA(cudaFreeAsync(tmp, g.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            return;
+        }
+        LGD_CHECK_CUDA(cudaMemcpy2DAsync(host, (size_t)g.desc.nx * helem, member_buf(g, member, which),
+                                         g.pitch_bytes[member], (size_t)g.desc.nx * helem, rows,
+                                         cudaMemcpyDeviceToHost, g.stream));
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+static void region_copy(lgd_handle *h, int member, const int *streaks, int n_streaks, void *host,
+                        size_t bytes, bool to_grid)
+{
+    Grid& g = grid_of(h);
+    check_member(g, member, 0);
+    LGD_REQUIRE(g.desc.cell != LGD_CELL_JACOBI7_F64_FIX, LGD_ERR_UNSUPPORTED,
+                "region copies of the fixed-point grid are not supported; download the whole grid");
+    const long long cells = stage_streaks(g, streaks, n_streaks);
+    const int elem = g.m[member].elem;
+    LGD_REQUIRE(bytes == (size_t)cells * elem, LGD_ERR_INVALID, "byte count does not match the streaks");
+    if (cells == 0) return;
+    LGD_REQUIRE(host != nullptr, LGD_ERR_INVALID, "null host buffer");
+    void *d = nullptr;
+    LGD_CHECK_CUDA(cudaMallocAsync(&d, bytes, g.stream));
+    if (to_grid) {
+        LGD_CHECK_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, g.stream));
+    }
+    launch_streak_copy(g, member, 0, g.d_streaks, g.d_streak_prefix, n_streaks, cells, d, to_grid);
+    if (!to_grid) {
+        LGD_CHECK_CUDA(cudaMemcpyAsync(host, d, bytes, cudaMemcpyDeviceToHost, g.stream));
+    }
+    LGD_CHECK_CUDA(cudaFreeAsync(d, g.stream));
+    LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+}
+
+int lgd_gpu_save_region(lgd_handle *h, int member, const int *streaks, int n_streaks, void *host, size_t bytes)
+{
+    return guard([&] { region_copy(h, member, streaks, n_streaks, host, bytes, false); });
+}
+
+int lgd_gpu_load_region(lgd_handle *h, int member, const int *streaks, int n_streaks, const void *host, size_t bytes)
+{
+    return guard([&] { region_copy(h, member, streaks, n_streaks, const_cast<void *>(host), bytes, true); });
+}
+
+int lgd_gpu_step(lgd_handle *h, unsigned nano_step, int count)
+{
+    (void)nano_step;   // the compiled cells have one nano step
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(count >= 0, LGD_ERR_INVALID, "negative step count");
+        if (count == 0) return;
+        switch (g.desc.cell) {
+        case LGD_CELL_JACOBI7_F64:
+        case LGD_CELL_JACOBI7_F64_FIX:
+        case LGD_CELL_JACOBI7_F32:
+            launch_jacobi7(g, count);
+            break;
+        case LGD_CELL_GOL_U8:
+            launch_gol(g, count);
+            break;
+        case LGD_CELL_VARCOEF_F32:
+        case LGD_CELL_VARCOEF_F64:
+            launch_varcoef(g, count);
+            break;
+        default: {
+            // cells without a whole-grid kernel: region update over all rows
+            std::vector<int> streaks;
+            streaks.reserve((size_t)g.desc.ny * g.desc.nz * 4);
+            for (int z = 0; z < g.desc.nz; ++z) {
+                for (int y = 0; y < g.desc.ny; ++y) {
+                    streaks.push_back(0);
+                    streaks.push_back(y);
+                    streaks.push_back(z);
+                    streaks.push_back(g.desc.nx);
+                }
+            }
+            const int n = (int)(streaks.size() / 4);
+            const long long cells = stage_streaks(g, streaks.data(), n);
+            for (int s = 0; s < count; ++s) {
+                launch_region(g, g.d_streaks, g.d_streak_prefix, n, cells);
+                g.cur = 1 - g.cur;
+            }
+        }
+        }
+    });
+}
+
+int lgd_gpu_update_region(lgd_handle *h, const int *streaks, int n_streaks, unsigned nano_step)
+{
+    (void)nano_step;
+    return guard([&] {
+        Grid& g = grid_of(h);
+        const long long cells = stage_streaks(g, streaks, n_streaks);
+        launch_region(g, g.d_streaks, g.d_streak_prefix, n_streaks, cells);
+    });
+}
+
+int lgd_gpu_swap(lgd_handle *h)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        g.cur = 1 - g.cur;
+    });
+}
+
+int lgd_gpu_fill_uniform(lgd_handle *h, int member, int which, uint64_t seed, int stream)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        LGD_REQUIRE(g.m[member].elem != 1, LGD_ERR_INVALID, "uniform fill needs a floating-point member");
+        if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
+            raise_fix_exp(g, 0);   // uniform values lie in [0, 1)
+            launch_fill(g, member, which, seed, stream, 2, 0.0, g.fix_exp);
+        } else {
+            launch_fill(g, member, which, seed, stream, 0, 0.0, 0);
+        }
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_fill_bernoulli(lgd_handle *h, int member, int which, uint64_t seed, int stream, double p)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        LGD_REQUIRE(g.m[member].elem == 1, LGD_ERR_INVALID, "Bernoulli fill needs a uint8 member");
+        launch_fill(g, member, which, seed, stream, 1, p, 0);
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        LGD_REQUIRE(sum != nullptr, LGD_ERR_INVALID, "null output");
+        // the checksum kernel reads through the current/next view
+        const int saved = g.cur;
+        if (which == 1 && !g.m[member].is_static) g.cur = 1 - g.cur;
+        try {
+            launch_checksum(g, member, 0, sum);
+        } catch (...) {
+            g.cur = saved;
+            throw;
+        }
+        g.cur = saved;
+    });
+}
+
+int lgd_gpu_synchronize(lgd_handle *h)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_device_ptr(lgd_handle *h, int member, int which, void **ptr, size_t *pitch_bytes)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        LGD_REQUIRE(ptr != nullptr, LGD_ERR_INVALID, "null output");
+        *ptr = member_buf(g, member, which);
+        if (pitch_bytes) *pitch_bytes = g.pitch_bytes[member];
+    });
+}
+
+int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(count != nullptr, LGD_ERR_INVALID, "null output");
+        *count = g.launches;
+    });
+}
+
+int lgd_gpu_set_time_block(lgd_handle *h, int depth)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(depth >= 0 && depth <= 64, LGD_ERR_INVALID, "time block depth out of range");
+        g.time_block = depth;
+    });
+}
+
+int lgd_gpu_stream(lgd_handle *h, void **stream)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(stream != nullptr, LGD_ERR_INVALID, "null output");
+        *stream = (void *)g.stream;
+    });
+}
+
+int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(exp != nullptr, LGD_ERR_INVALID, "null output");
+        LGD_REQUIRE(g.desc.cell == LGD_CELL_JACOBI7_F64_FIX, LGD_ERR_INVALID, "not a fixed-point grid");
+        *exp = g.fix_exp;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+// Device-side helpers shared by the kernels: pitched grid views, boundary
+// handling (constant edge cell or periodic wrap, the reference's Cube and
+// Torus topologies, geometry/topologies.h:179-278) and the per-cell update
+// rules used by the generic (region) kernels.
+#ifndef LGD_K_COMMON_CUH
+#define LGD_K_COMMON_CUH
+
+#include <stdint.h>
+
+namespace lgd {
+
+// A pitched 3D array: element (x, y, z) at p[(z * ny + y) * pitch + x].
+template<typename T>
+struct View {
+    T *p;
+    long pitch;
+    int nx, ny, nz;
+    __host__ __device__ T *row(int y, int z) const { return p + ((long)z * ny + y) * pitch; }
+    __host__ __device__ T& at(int x, int y, int z) const { return p[((long)z * ny + y) * pitch + x]; }
+};
+
+__device__ __forceinline__ int wrap_axis(int i, int n)
+{
+    return (i < 0) ? i + n : ((i >= n) ? i - n : i);
+}
+
+// Value at (x, y, z) for a neighbour at most one cell outside the box:
+// wrapped on periodic axes, the edge value on the others.
+template<typename T>
+__device__ __forceinline__ T load_bc(const View<const T>& v, int x, int y, int z, int periodic, T edge)
+{
+    if (x < 0 || x >= v.nx) {
+        if (!(periodic & 1)) return edge;
+        x = wrap_axis(x, v.nx);
+    }
+    if (y < 0 || y >= v.ny) {
+        if (!(periodic & 2)) return edge;
+        y = wrap_axis(y, v.ny);
+    }
+    if (z < 0 || z >= v.nz) {
+        if (!(periodic & 4)) return edge;
+        z = wrap_axis(z, v.nz);
+    }
+    return v.at(x, y, z);
+}
+
+// ---- SplitMix64 (matches libgeodecomp_gb300/workloads.py)
+__host__ __device__ __forceinline__ uint64_t splitmix_mix(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ double splitmix_uniform(uint64_t key, uint64_t i)
+{
+    uint64_t r = splitmix_mix(key + (i + 1) * 0x9E3779B97F4A7C15ull);
+    return (double)(r >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ---- fixed-point representation of the FP64 Jacobi grid
+// value = k * 2^(scale_exp - 60), k a signed 64-bit integer, |value| <= 2^scale_exp.
+// The averaging stencil maps [-S, S] into itself, so 7 * 2^60 bounds every
+// neighbour sum and nothing overflows.
+__device__ __forceinline__ long long fx_div7_round(long long sum)
+{
+    // round(sum / 7) with ties towards +inf, via an unsigned offset so that
+    // the division is a multiply-high (sum is in [-7*2^60, 7*2^60]).
+    const unsigned long long off = 7ull << 60;
+    unsigned long long n = (unsigned long long)(sum + 3) + off;
+    unsigned long long t = __umul64hi(n, 0x2492492492492493ull);
+    unsigned long long q = (((n - t) >> 1) + t) >> 2;
+    return (long long)(q - (1ull << 60));
+}
+
+}  // namespace lgd
+
+#endif

@@ -1,0 +1,221 @@
+// Whole-grid 3D seven-point kernels (Jacobi-7 in FP64 / FP32 / 64-bit
+// fixed point, variable-coefficient diffusion).
+//
+// 2.5D blocking: a CTA owns a BX x BY column of cells and marches along z.
+// The plane being updated sits in shared memory with a one-cell halo (for
+// the four in-plane neighbours); the planes below and above stay in
+// registers, so every cell is read from memory once per plane sweep plus
+// the halo re-reads, which hit L2.  Algorithmic traffic: one read and one
+// write per cell and step (16 B/cell for FP64, 8 B for FP32; varcoef adds
+// the coefficient read).
+#include "lgd_internal.h"
+#include "k_cells.cuh"
+
+namespace lgd {
+
+static const int SBX = 32;
+static const int SBY = 8;
+
+// Value at arbitrary (x, y, z) within one grid extent outside the box:
+// periodic axes wrap by modulo, the others return the edge value.
+template<typename T>
+__device__ __forceinline__ T load_any(const View<const T>& v, int x, int y, int z, int periodic, T edge)
+{
+    if ((unsigned)x >= (unsigned)v.nx) {
+        if (!(periodic & 1)) return edge;
+        x = ((x % v.nx) + v.nx) % v.nx;
+    }
+    if ((unsigned)y >= (unsigned)v.ny) {
+        if (!(periodic & 2)) return edge;
+        y = ((y % v.ny) + v.ny) % v.ny;
+    }
+    if ((unsigned)z >= (unsigned)v.nz) {
+        if (!(periodic & 4)) return edge;
+        z = ((z % v.nz) + v.nz) % v.nz;
+    }
+    return v.at(x, y, z);
+}
+
+template<typename CELL>
+__global__ void __launch_bounds__(SBX * SBY)
+jacobi7_zmarch_kernel(View<const typename CELL::T> in, View<typename CELL::T> out, int periodic,
+                      typename CELL::T edge, int zchunk)
+{
+    typedef typename CELL::T T;
+    __shared__ T tile[SBY + 2][SBX + 2];
+    const int tx = threadIdx.x;
+    const int ty = threadIdx.y;
+    const int x = blockIdx.x * SBX + tx;
+    const int y = blockIdx.y * SBY + ty;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, in.nz);
+    const bool inside = (x < in.nx) && (y < in.ny);
+
+    T below = load_any(in, x, y, z0 - 1, periodic, edge);
+    T cur = load_any(in, x, y, z0, periodic, edge);
+    for (int z = z0; z < z1; ++z) {
+        T above = (inside && z + 1 < in.nz) ? in.at(x, y, z + 1) : load_any(in, x, y, z + 1, periodic, edge);
+        tile[ty + 1][tx + 1] = cur;
+        if (tx == 0) tile[ty + 1][0] = load_any(in, x - 1, y, z, periodic, edge);
+        if (tx == SBX - 1) tile[ty + 1][SBX + 1] = load_any(in, x + 1, y, z, periodic, edge);
+        if (ty == 0) tile[0][tx + 1] = load_any(in, x, y - 1, z, periodic, edge);
+        if (ty == SBY - 1) tile[SBY + 1][tx + 1] = load_any(in, x, y + 1, z, periodic, edge);
+        __syncthreads();
+        if (inside) {
+            out.at(x, y, z) = CELL::apply(cur, tile[ty][tx + 1], tile[ty + 2][tx + 1], tile[ty + 1][tx + 2],
+                                          tile[ty + 1][tx], above, below);
+        }
+        __syncthreads();
+        below = cur;
+        cur = above;
+    }
+}
+
+template<typename R>
+__global__ void __launch_bounds__(SBX * SBY)
+varcoef_zmarch_kernel(View<const R> u, View<const R> k, View<R> out, int periodic, R edgeU, R edgeK, int zchunk)
+{
+    __shared__ R tu[SBY + 2][SBX + 2];
+    __shared__ R tk[SBY + 2][SBX + 2];
+    const int tx = threadIdx.x;
+    const int ty = threadIdx.y;
+    const int x = blockIdx.x * SBX + tx;
+    const int y = blockIdx.y * SBY + ty;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, u.nz);
+    const bool inside = (x < u.nx) && (y < u.ny);
+
+    R ub = load_any(u, x, y, z0 - 1, periodic, edgeU);
+    R kb = load_any(k, x, y, z0 - 1, periodic, edgeK);
+    R uc = load_any(u, x, y, z0, periodic, edgeU);
+    R kc = load_any(k, x, y, z0, periodic, edgeK);
+    for (int z = z0; z < z1; ++z) {
+        R ut = load_any(u, x, y, z + 1, periodic, edgeU);
+        R kt = load_any(k, x, y, z + 1, periodic, edgeK);
+        tu[ty + 1][tx + 1] = uc;
+        tk[ty + 1][tx + 1] = kc;
+        if (tx == 0) {
+            tu[ty + 1][0] = load_any(u, x - 1, y, z, periodic, edgeU);
+            tk[ty + 1][0] = load_any(k, x - 1, y, z, periodic, edgeK);
+        }
+        if (tx == SBX - 1) {
+            tu[ty + 1][SBX + 1] = load_any(u, x + 1, y, z, periodic, edgeU);
+            tk[ty + 1][SBX + 1] = load_any(k, x + 1, y, z, periodic, edgeK);
+        }
+        if (ty == 0) {
+            tu[0][tx + 1] = load_any(u, x, y - 1, z, periodic, edgeU);
+            tk[0][tx + 1] = load_any(k, x, y - 1, z, periodic, edgeK);
+        }
+        if (ty == SBY - 1) {
+            tu[SBY + 1][tx + 1] = load_any(u, x, y + 1, z, periodic, edgeU);
+            tk[SBY + 1][tx + 1] = load_any(k, x, y + 1, z, periodic, edgeK);
+        }
+        __syncthreads();
+        if (inside) {
+            out.at(x, y, z) = VarCoef<R>::apply(
+                uc, kc,
+                tu[ty + 1][tx], tk[ty + 1][tx],            // -x
+                tu[ty + 1][tx + 2], tk[ty + 1][tx + 2],    // +x
+                tu[ty][tx + 1], tk[ty][tx + 1],            // -y
+                tu[ty + 2][tx + 1], tk[ty + 2][tx + 1],    // +y
+                ub, kb,                                    // -z
+                ut, kt);                                   // +z
+        }
+        __syncthreads();
+        ub = uc;
+        kb = kc;
+        uc = ut;
+        kc = kt;
+    }
+}
+
+template<typename T>
+static View<T> mview(Grid& g, int member, int which)
+{
+    View<T> v;
+    v.p = (T *)g.m[member].buf[g.m[member].is_static ? 0 : (which ? 1 - g.cur : g.cur)];
+    v.pitch = (long)(g.pitch_bytes[member] / sizeof(T));
+    v.nx = g.desc.nx;
+    v.ny = g.desc.ny;
+    v.nz = g.desc.nz;
+    return v;
+}
+
+template<typename T>
+static View<const T> cmview(Grid& g, int member, int which)
+{
+    View<T> v = mview<T>(g, member, which);
+    View<const T> c;
+    c.p = v.p;
+    c.pitch = v.pitch;
+    c.nx = v.nx;
+    c.ny = v.ny;
+    c.nz = v.nz;
+    return c;
+}
+
+static dim3 zmarch_grid(const Grid& g, int *zchunk)
+{
+    const int bx = (g.desc.nx + SBX - 1) / SBX;
+    const int by = (g.desc.ny + SBY - 1) / SBY;
+    const long long xy = (long long)bx * by;
+    // enough CTAs to fill 152 SMs several times over, z chunks of >= 8 planes
+    int zsplit = (int)((152LL * 8 + xy - 1) / xy);
+    zsplit = max(1, min(zsplit, (g.desc.nz + 7) / 8));
+    *zchunk = (g.desc.nz + zsplit - 1) / zsplit;
+    zsplit = (g.desc.nz + *zchunk - 1) / *zchunk;
+    return dim3(bx, by, zsplit);
+}
+
+long long fix_edge(const Grid& g);
+
+void launch_jacobi7(Grid& g, int steps)
+{
+    int zchunk = 1;
+    dim3 grid = zmarch_grid(g, &zchunk);
+    dim3 block(SBX, SBY);
+    for (int s = 0; s < steps; ++s) {
+        switch (g.desc.cell) {
+        case LGD_CELL_JACOBI7_F64:
+            jacobi7_zmarch_kernel<Jacobi7F64><<<grid, block, 0, g.stream>>>(
+                cmview<double>(g, 0, 0), mview<double>(g, 0, 1), g.desc.periodic, g.desc.edge[0], zchunk);
+            break;
+        case LGD_CELL_JACOBI7_F32:
+            jacobi7_zmarch_kernel<Jacobi7F32><<<grid, block, 0, g.stream>>>(
+                cmview<float>(g, 0, 0), mview<float>(g, 0, 1), g.desc.periodic, (float)g.desc.edge[0], zchunk);
+            break;
+        case LGD_CELL_JACOBI7_F64_FIX:
+            jacobi7_zmarch_kernel<Jacobi7Fix><<<grid, block, 0, g.stream>>>(
+                cmview<long long>(g, 0, 0), mview<long long>(g, 0, 1), g.desc.periodic, fix_edge(g), zchunk);
+            break;
+        default:
+            throw Error(LGD_ERR_UNSUPPORTED, "not a Jacobi cell");
+        }
+        check_launch("jacobi7");
+        ++g.launches;
+        g.cur = 1 - g.cur;
+    }
+}
+
+void launch_varcoef(Grid& g, int steps)
+{
+    int zchunk = 1;
+    dim3 grid = zmarch_grid(g, &zchunk);
+    dim3 block(SBX, SBY);
+    for (int s = 0; s < steps; ++s) {
+        if (g.desc.cell == LGD_CELL_VARCOEF_F32) {
+            varcoef_zmarch_kernel<float><<<grid, block, 0, g.stream>>>(
+                cmview<float>(g, 0, 0), cmview<float>(g, 1, 0), mview<float>(g, 0, 1), g.desc.periodic,
+                (float)g.desc.edge[0], (float)g.desc.edge[1], zchunk);
+        } else {
+            varcoef_zmarch_kernel<double><<<grid, block, 0, g.stream>>>(
+                cmview<double>(g, 0, 0), cmview<double>(g, 1, 0), mview<double>(g, 0, 1), g.desc.periodic,
+                g.desc.edge[0], g.desc.edge[1], zchunk);
+        }
+        check_launch("varcoef");
+        ++g.launches;
+        g.cur = 1 - g.cur;
+    }
+}
+
+}  // namespace lgd

@@ -1,0 +1,120 @@
+// Internal declarations shared by the library's translation units.
+#ifndef LGD_INTERNAL_H
+#define LGD_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+
+#include "../../include/lgd_gpu.h"
+
+namespace lgd {
+
+// Exceptions used inside the library; lgd_guard() maps them to status codes.
+struct Error : std::runtime_error {
+    int code;
+    Error(int code, const std::string& msg) : std::runtime_error(msg), code(code) {}
+};
+
+void set_error(int code, const std::string& msg);
+void clear_error();
+
+#define LGD_CHECK_CUDA(expr)                                                               \
+    do {                                                                                   \
+        cudaError_t lgd_err_ = (expr);                                                     \
+        if (lgd_err_ != cudaSuccess) {                                                     \
+            throw ::lgd::Error(LGD_ERR_CUDA, std::string("CUDA error: ") +                 \
+                               cudaGetErrorString(lgd_err_) + " at " #expr);               \
+        }                                                                                  \
+    } while (0)
+
+#define LGD_REQUIRE(cond, code, msg)                                                       \
+    do {                                                                                   \
+        if (!(cond)) {                                                                     \
+            throw ::lgd::Error((code), (msg));                                             \
+        }                                                                                  \
+    } while (0)
+
+// Runs f, converting exceptions into status codes and the thread's last
+// error message.
+template<typename F>
+int guard(F&& f)
+{
+    try {
+        clear_error();
+        f();
+        return LGD_OK;
+    } catch (const Error& e) {
+        set_error(e.code, e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_error(LGD_ERR_NOMEM, "host allocation failed");
+        return LGD_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        set_error(LGD_ERR_INVALID, e.what());
+        return LGD_ERR_INVALID;
+    }
+}
+
+// Throws if the last launch failed to start.
+inline void check_launch(const char *what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        throw Error(LGD_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e) + " launching " + what);
+    }
+}
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// One structured grid: SoA members, each double-buffered and pitched so
+// that every row starts on a 128-byte boundary.
+struct Member {
+    int elem;           // bytes per element
+    bool is_static;     // never written by the cell (one buffer serves both)
+    void *buf[2];
+};
+
+struct Grid {
+    lgd_grid_desc desc;
+    int n_members;
+    Member m[2];
+    size_t pitch_elems;     // row pitch in elements (same for all members of equal size)
+    size_t pitch_bytes[2];  // per member
+    size_t plane_elems;     // pitch_elems * ny
+    int cur;                // index of the current buffer
+    int time_block;         // temporal blocking depth (0 = default)
+    int fix_exp;            // fixed-point grids: value = k * 2^(fix_exp - 60)
+    cudaStream_t stream;
+    uint64_t launches;
+    int device;
+    // scratch for region updates and reductions
+    int *d_streaks;
+    long long *d_streak_prefix;
+    int streak_capacity;
+    double *d_partials;
+    int partial_capacity;
+};
+
+// kernels, one entry per cell family (implemented in k_*.cu)
+void launch_jacobi7(Grid& g, int steps);
+void launch_gol(Grid& g, int steps);
+void launch_varcoef(Grid& g, int steps);
+void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells);
+void launch_fill(Grid& g, int member, int which, uint64_t seed, int stream, int mode, double p, int scale_exp);
+void launch_checksum(Grid& g, int member, int which, double *out);
+void launch_streak_copy(Grid& g, int member, int which, const int *d_streaks, const long long *d_prefix,
+                        int n_streaks, long long cells, void *d_packed, bool to_grid);
+
+// SplitMix64 key derivation shared with the fill kernel
+uint64_t stream_key(uint64_t seed, int stream);
+
+}  // namespace lgd
+
+struct lgd_handle {
+    lgd::Grid g;
+};
+
+#endif

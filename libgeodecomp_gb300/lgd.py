@@ -1,0 +1,221 @@
+"""ctypes binding of the C ABI in include/lgd_gpu.h.
+
+Used by the tests and the benchmark.  Loading fails loudly when the CUDA
+library has not been built: there is no CPU fallback anywhere on this path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblgd_gb300.so")
+
+OK = 0
+ERR_INVALID = 1
+ERR_RANGE = 2
+ERR_CUDA = 3
+ERR_NOMEM = 4
+ERR_TIMEOUT = 5
+ERR_UNSUPPORTED = 6
+
+CELL_JACOBI7_F64 = 1
+CELL_JACOBI7_F64_FIX = 2
+CELL_JACOBI7_F32 = 3
+CELL_SUM6_F64 = 4
+CELL_GOL_U8 = 5
+CELL_VARCOEF_F32 = 6
+CELL_VARCOEF_F64 = 7
+
+# host dtype of each member, per cell kind
+MEMBERS = {
+    CELL_JACOBI7_F64: [np.float64],
+    CELL_JACOBI7_F64_FIX: [np.float64],
+    CELL_JACOBI7_F32: [np.float32],
+    CELL_SUM6_F64: [np.float64, np.float64],
+    CELL_GOL_U8: [np.uint8],
+    CELL_VARCOEF_F32: [np.float32, np.float32],
+    CELL_VARCOEF_F64: [np.float64, np.float64],
+}
+
+
+class LGDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("lgd error %d: %s" % (code, msg))
+        self.code = code
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("periodic", ctypes.c_int), ("cell", ctypes.c_int), ("flags", ctypes.c_int),
+                ("edge", ctypes.c_double * 4)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if it is missing (build it with
+    ``python -c "import __graft_entry__ as g; g.build()"``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("CUDA library %s is not built" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        S = ctypes.c_size_t
+        U64 = ctypes.c_uint64
+        for name, args in {
+            "lgd_gpu_last_error": [ctypes.c_char_p, S],
+            "lgd_gpu_version": [],
+            "lgd_gpu_device_count": [P],
+            "lgd_gpu_create": [P, P],
+            "lgd_gpu_destroy": [P],
+            "lgd_gpu_upload": [P, I, I, P, S],
+            "lgd_gpu_download": [P, I, I, P, S],
+            "lgd_gpu_save_region": [P, I, P, I, P, S],
+            "lgd_gpu_load_region": [P, I, P, I, P, S],
+            "lgd_gpu_step": [P, ctypes.c_uint, I],
+            "lgd_gpu_update_region": [P, P, I, ctypes.c_uint],
+            "lgd_gpu_swap": [P],
+            "lgd_gpu_fill_uniform": [P, I, I, U64, I],
+            "lgd_gpu_fill_bernoulli": [P, I, I, U64, I, ctypes.c_double],
+            "lgd_gpu_fixed_point_exponent": [P, P],
+            "lgd_gpu_checksum": [P, I, I, P],
+            "lgd_gpu_synchronize": [P],
+            "lgd_gpu_device_ptr": [P, I, I, P, P],
+            "lgd_gpu_launch_count": [P, P],
+            "lgd_gpu_set_time_block": [P, I],
+        }.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = I
+        _lib = L
+    return _lib
+
+
+def check(rc: int):
+    if rc != OK:
+        buf = ctypes.create_string_buffer(512)
+        lib().lgd_gpu_last_error(buf, 512)
+        raise LGDError(rc, buf.value.decode(errors="replace"))
+
+
+def device_count() -> int:
+    n = ctypes.c_int(0)
+    check(lib().lgd_gpu_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Grid:
+    """One structured device grid (a handle of the C ABI)."""
+
+    def __init__(self, cell: int, shape, periodic: int = 0, edge=(0.0, 0.0, 0.0, 0.0)):
+        shape = tuple(int(s) for s in shape)
+        if len(shape) == 2:
+            ny, nx = shape
+            nz, dim = 1, 2
+        else:
+            nz, ny, nx = shape
+            dim = 3
+        d = GridDesc()
+        d.dim, d.nx, d.ny, d.nz = dim, nx, ny, nz
+        d.periodic, d.cell, d.flags = periodic, cell, 0
+        for i, e in enumerate(list(edge)[:4]):
+            d.edge[i] = float(e)
+        self.cell = cell
+        self.shape = shape
+        self.cells = nx * ny * nz
+        self.members = MEMBERS.get(cell, [])
+        self._h = ctypes.c_void_p()
+        check(lib().lgd_gpu_create(ctypes.byref(d), ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            check(lib().lgd_gpu_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, member: int, values: np.ndarray, which: int = 0):
+        a = np.ascontiguousarray(values, dtype=self.members[member])
+        assert a.size == self.cells
+        check(lib().lgd_gpu_upload(self._h, member, which, _ptr(a), a.nbytes))
+
+    def download(self, member: int = 0, which: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.shape, dtype=self.members[member])
+        check(lib().lgd_gpu_download(self._h, member, which, _ptr(out), out.nbytes))
+        return out
+
+    def step(self, count: int = 1, nano_step: int = 0):
+        check(lib().lgd_gpu_step(self._h, nano_step, count))
+
+    def update_region(self, streaks, nano_step: int = 0):
+        s = np.ascontiguousarray(np.asarray(streaks, dtype=np.int32).reshape(-1, 4))
+        check(lib().lgd_gpu_update_region(self._h, _ptr(s), s.shape[0], nano_step))
+
+    def swap(self):
+        check(lib().lgd_gpu_swap(self._h))
+
+    def save_region(self, member: int, streaks) -> np.ndarray:
+        s = np.ascontiguousarray(np.asarray(streaks, dtype=np.int32).reshape(-1, 4))
+        n = int((s[:, 3] - s[:, 0]).sum())
+        out = np.empty(n, dtype=self.members[member])
+        check(lib().lgd_gpu_save_region(self._h, member, _ptr(s), s.shape[0], _ptr(out), out.nbytes))
+        return out
+
+    def load_region(self, member: int, streaks, values: np.ndarray):
+        s = np.ascontiguousarray(np.asarray(streaks, dtype=np.int32).reshape(-1, 4))
+        v = np.ascontiguousarray(values, dtype=self.members[member])
+        check(lib().lgd_gpu_load_region(self._h, member, _ptr(s), s.shape[0], _ptr(v), v.nbytes))
+
+    def fill_uniform(self, member: int = 0, seed: int = 42, stream: int = 1, which: int = 0):
+        check(lib().lgd_gpu_fill_uniform(self._h, member, which, seed, stream))
+
+    def fill_bernoulli(self, p: float, member: int = 0, seed: int = 42, stream: int = 1, which: int = 0):
+        check(lib().lgd_gpu_fill_bernoulli(self._h, member, which, seed, stream, p))
+
+    def checksum(self, member: int = 0, which: int = 0) -> float:
+        s = ctypes.c_double()
+        check(lib().lgd_gpu_checksum(self._h, member, which, ctypes.byref(s)))
+        return s.value
+
+    def synchronize(self):
+        check(lib().lgd_gpu_synchronize(self._h))
+
+    def device_ptr(self, member: int = 0, which: int = 0):
+        p = ctypes.c_void_p()
+        pitch = ctypes.c_size_t()
+        check(lib().lgd_gpu_device_ptr(self._h, member, which, ctypes.byref(p), ctypes.byref(pitch)))
+        return p.value, pitch.value
+
+    def launch_count(self) -> int:
+        n = ctypes.c_uint64()
+        check(lib().lgd_gpu_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def set_time_block(self, depth: int):
+        check(lib().lgd_gpu_set_time_block(self._h, depth))
+
+    def fixed_point_exponent(self) -> int:
+        e = ctypes.c_int()
+        check(lib().lgd_gpu_fixed_point_exponent(self._h, ctypes.byref(e)))
+        return e.value

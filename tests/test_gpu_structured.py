@@ -1,0 +1,292 @@
+"""Structured-grid parity on the GPU, through the C ABI.
+
+Integer and IEEE-FP64 cells must match the reference bit for bit; the
+fixed-point FP64 Jacobi must stay within 1e-12 relative of the FP64
+reference; FP32 cells state their error against the FP64 oracle.  The
+boundary-handling cases restate the reference's own known-answer test
+(storage/test/unit/fixedneighborhoodupdatefunctortest.h:109-379).
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from libgeodecomp_gb300 import lgd, workloads
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name + ".npz"), allow_pickle=False)
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run_grid(cell, arrays, steps, periodic=0, edge=(0.0, 0.0, 0.0, 0.0), member=0):
+    shape = arrays[0].shape
+    with lgd.Grid(cell, shape, periodic=periodic, edge=edge) as g:
+        for m, a in enumerate(arrays):
+            g.upload(m, a)
+        g.step(steps)
+        return g.download(member)
+
+
+# ------------------------------------------------------------------ Jacobi-7
+@pytest.mark.parametrize("name", ["jacobi7_cube_24x20x16", "jacobi7_torus_17x13x11"])
+def test_jacobi7_f64_bit_exact_small(name):
+    g = load(name)
+    nz, ny, nx = g["shape"]
+    u0 = workloads.jacobi_initial(nx, ny, nz, seed=42)
+    out = run_grid(lgd.CELL_JACOBI7_F64, [u0], int(g["steps"]), periodic=7 if bool(g["torus"]) else 0)
+    np.testing.assert_array_equal(out, g["out"])
+
+
+def test_jacobi7_f64_bit_exact_128_config():
+    g = load("jacobi7_cube_128")
+    u0 = workloads.jacobi_initial(128, 128, 128, seed=42)
+    out = run_grid(lgd.CELL_JACOBI7_F64, [u0], 100)
+    np.testing.assert_array_equal(out.reshape(-1)[g["sample_idx"]], g["sample"])
+    assert sha(out) == str(g["sha256"])
+
+
+@pytest.mark.parametrize("shape,periodic", [((13, 11, 7), 0), ((5, 9, 33), 7), ((1, 10, 20), 7), ((40, 3, 65), 2)])
+def test_jacobi7_f64_odd_shapes_match_oracle(shape, periodic):
+    u0 = workloads.jacobi_initial(shape[2], shape[1], shape[0], seed=5)
+    if periodic not in (0, 7):
+        pytest.skip("the oracle has cube or full torus only")
+    out = run_grid(lgd.CELL_JACOBI7_F64, [u0], 9, periodic=periodic)
+    np.testing.assert_array_equal(out, oracle.jacobi7(u0, 9, torus=periodic == 7))
+
+
+def test_jacobi7_f64_nonzero_edge():
+    u0 = workloads.jacobi_initial(20, 12, 9, seed=8)
+    out = run_grid(lgd.CELL_JACOBI7_F64, [u0], 6, edge=(0.75, 0, 0, 0))
+    np.testing.assert_array_equal(out, oracle.jacobi7(u0, 6, edge=0.75))
+
+
+def rel_err(a, b):
+    return np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+
+
+def test_jacobi7_fixed_point_within_1e12_of_reference_128_config():
+    g = load("jacobi7_cube_128")
+    u0 = workloads.jacobi_initial(128, 128, 128, seed=42)
+    out = run_grid(lgd.CELL_JACOBI7_F64_FIX, [u0], 100)
+    ref = oracle.jacobi7(u0, 100)
+    assert sha(ref) == str(g["sha256"])
+    assert rel_err(out, ref) <= 1e-12
+    np.testing.assert_allclose(out.reshape(-1)[g["sample_idx"]], g["sample"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("name", ["jacobi7_cube_24x20x16", "jacobi7_torus_17x13x11"])
+def test_jacobi7_fixed_point_small(name):
+    g = load(name)
+    nz, ny, nx = g["shape"]
+    u0 = workloads.jacobi_initial(nx, ny, nz, seed=42)
+    out = run_grid(lgd.CELL_JACOBI7_F64_FIX, [u0], int(g["steps"]), periodic=7 if bool(g["torus"]) else 0)
+    assert rel_err(out, g["out"]) <= 1e-12
+
+
+def test_jacobi7_fixed_point_signed_values_and_edge():
+    u0 = workloads.jacobi_initial(31, 17, 12, seed=9) * 6.0 - 3.0
+    out = run_grid(lgd.CELL_JACOBI7_F64_FIX, [u0], 20, edge=(-2.5, 0, 0, 0))
+    ref = oracle.jacobi7(u0, 20, edge=-2.5)
+    # error bound: 20 steps x half a unit of 2^(e - 60), e = 2 (values < 4)
+    assert np.max(np.abs(out - ref)) <= 20 * 2.0 ** (2 - 61)
+
+
+def test_jacobi7_fixed_point_device_fill_matches_host_generator():
+    with lgd.Grid(lgd.CELL_JACOBI7_F64_FIX, (16, 16, 16)) as g:
+        g.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
+        got = g.download(0)
+    np.testing.assert_array_equal(got, workloads.jacobi_initial(16, 16, 16, seed=42))
+
+
+def test_jacobi7_f32_error_against_fp64():
+    u0 = workloads.jacobi_initial(64, 64, 64, seed=42)
+    out = run_grid(lgd.CELL_JACOBI7_F32, [u0.astype(np.float32)], 50).astype(np.float64)
+    ref = oracle.jacobi7(u0, 50)
+    rel_l2 = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    max_abs = np.max(np.abs(out - ref))
+    assert rel_l2 < 2e-6 and max_abs < 2e-6, (rel_l2, max_abs)
+
+
+# ---------------------------------------- boundary handling (reference KAT)
+def coord_values(nz, ny, nx, origin):
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    return (x + origin[0]) + (y + origin[1]) * 1000.0 + (z + origin[2]) * 1000.0 * 1000.0
+
+
+def expected_sum6(nz, ny, nx, origin, streaks, torus):
+    """The reference test's expectation: the coordinate-encoded sum over the
+    six face neighbours, normalised on the torus, (-1,-1,-1) off the cube."""
+    exp = {}
+    for (x0, y, z, end) in streaks:
+        for x in range(x0, end):
+            sx = sy = sz = 0
+            for d in ((0, 0, -1), (0, -1, 0), (-1, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)):
+                cx, cy, cz = x + d[0], y + d[1], z + d[2]
+                if torus:
+                    cx, cy, cz = cx % nx, cy % ny, cz % nz
+                    sx += cx + origin[0]
+                    sy += cy + origin[1]
+                    sz += cz + origin[2]
+                elif 0 <= cx < nx and 0 <= cy < ny and 0 <= cz < nz:
+                    sx += cx + origin[0]
+                    sy += cy + origin[1]
+                    sz += cz + origin[2]
+                else:
+                    sx -= 1
+                    sy -= 1
+                    sz -= 1
+            exp[(x, y, z)] = sx + sy * 1000.0 + sz * 1000 * 1000.0
+    return exp
+
+
+# the reference test's region, shifted to the box origin (10, 20, 30)
+REF_STREAKS = [(10, 20, 30, 209), (10, 21, 30, 210), (10, 30, 30, 210), (10, 30, 40, 210),
+               (25, 31, 40, 200), (25, 119, 40, 200), (10, 30, 49, 210)]
+
+
+@pytest.mark.parametrize("torus", [True, False])
+def test_sum6_reference_region_kat(torus):
+    origin = (10, 20, 30)
+    nx, ny, nz = 200, 100, 50
+    streaks = [(x - origin[0], y - origin[1], z - origin[2], e - origin[0]) for (x, y, z, e) in REF_STREAKS]
+    a = coord_values(nz, ny, nx, origin)
+    edge = (-1001001.0, -1.0, 0, 0)
+    with lgd.Grid(lgd.CELL_SUM6_F64, (nz, ny, nx), periodic=7 if torus else 0, edge=edge) as g:
+        g.upload(0, a)
+        g.upload(1, np.full(a.shape, 777.0))
+        g.upload(1, np.full(a.shape, 999.0), which=1)
+        g.update_region(streaks)
+        g.swap()
+        b = g.download(1)
+    exp = expected_sum6(nz, ny, nx, origin, streaks, torus)
+    for (x, y, z), v in exp.items():
+        assert b[z, y, x] == v, (x, y, z)
+    # cells outside the region keep the new grid's previous contents
+    mask = np.ones(b.shape, dtype=bool)
+    for (x, y, z) in exp:
+        mask[z, y, x] = False
+    assert np.all(b[mask] == 999.0)
+
+
+def test_sum6_degenerated_torus_kat():
+    nx, ny, nz = 1, 10, 20
+    a = coord_values(nz, ny, nx, (0, 0, 0))
+    streaks = [(0, y, z, 1) for z in range(nz) for y in range(ny)]
+    with lgd.Grid(lgd.CELL_SUM6_F64, (nz, ny, nx), periodic=7) as g:
+        g.upload(0, a)
+        g.update_region(streaks)
+        g.swap()
+        b = g.download(1)
+    exp = expected_sum6(nz, ny, nx, (0, 0, 0), streaks, True)
+    for (x, y, z), v in exp.items():
+        assert b[z, y, x] == v
+
+
+def test_region_rejects_streaks_outside_the_grid():
+    with lgd.Grid(lgd.CELL_JACOBI7_F64, (4, 4, 4)) as g:
+        with pytest.raises(lgd.LGDError) as e:
+            g.update_region([(0, 0, 0, 5)])
+        assert e.value.code == lgd.ERR_RANGE
+        with pytest.raises(lgd.LGDError) as e:
+            g.update_region([(0, 4, 0, 1)])
+        assert e.value.code == lgd.ERR_RANGE
+
+
+def test_upload_rejects_wrong_size():
+    with lgd.Grid(lgd.CELL_JACOBI7_F64, (4, 4, 4)) as g:
+        with pytest.raises(lgd.LGDError) as e:
+            lgd.check(lgd.lib().lgd_gpu_upload(g._h, 0, 0, lgd._ptr(np.zeros(10)), 80))
+        assert e.value.code == lgd.ERR_INVALID
+
+
+def test_region_save_load_roundtrip():
+    u0 = workloads.jacobi_initial(30, 20, 10, seed=4)
+    streaks = [(3, 2, 1, 17), (0, 19, 9, 30), (5, 5, 5, 6)]
+    with lgd.Grid(lgd.CELL_JACOBI7_F64, u0.shape) as g:
+        g.upload(0, u0)
+        got = g.save_region(0, streaks)
+        exp = np.concatenate([u0[z, y, x:e] for (x, y, z, e) in streaks])
+        np.testing.assert_array_equal(got, exp)
+        g.load_region(0, streaks, -got)
+        u1 = g.download(0)
+    ref = u0.copy()
+    for (x, y, z, e) in streaks:
+        ref[z, y, x:e] = -ref[z, y, x:e]
+    np.testing.assert_array_equal(u1, ref)
+
+
+def test_checksum_matches_host_sum():
+    u0 = workloads.jacobi_initial(50, 40, 30, seed=2)
+    with lgd.Grid(lgd.CELL_JACOBI7_F64, u0.shape) as g:
+        g.upload(0, u0)
+        assert abs(g.checksum(0) - u0.sum()) <= 1e-9 * u0.sum()
+
+
+# ------------------------------------------------------------- Game of Life
+def test_gol_small_bit_exact():
+    g = load("gol_64x48")
+    c0 = workloads.gol_initial(64, 48, seed=42)
+    np.testing.assert_array_equal(run_grid(lgd.CELL_GOL_U8, [c0], 50, periodic=3), g["out"])
+
+
+def test_gol_1024_1000_steps_golden():
+    g = load("gol_1024")
+    c0 = workloads.gol_initial(1024, 1024, seed=42)
+    out = run_grid(lgd.CELL_GOL_U8, [c0], 1000, periodic=3)
+    np.testing.assert_array_equal(out.sum(axis=1), g["row_alive"])
+    assert sha(out) == str(g["sha256"])
+
+
+@pytest.mark.parametrize("shape", [(37, 50), (1, 16), (3, 3), (17, 48)])
+def test_gol_odd_shapes_match_oracle(shape):
+    c0 = workloads.gol_initial(shape[1], shape[0], seed=6)
+    np.testing.assert_array_equal(run_grid(lgd.CELL_GOL_U8, [c0], 23, periodic=3), oracle.gol(c0, 23))
+
+
+def gol_cube_numpy(c, steps):
+    c = c.astype(np.int32)
+    for _ in range(steps):
+        p = np.pad(c, 1)
+        n = sum(p[1 + dy:1 + dy + c.shape[0], 1 + dx:1 + dx + c.shape[1]]
+                for dy in (-1, 0, 1) for dx in (-1, 0, 1) if (dy, dx) != (0, 0))
+        c = np.where(c == 1, ((n == 2) | (n == 3)), n == 3).astype(np.int32)
+    return c.astype(np.uint8)
+
+
+def test_gol_cube_dead_edge():
+    c0 = workloads.gol_initial(45, 31, seed=3)
+    np.testing.assert_array_equal(run_grid(lgd.CELL_GOL_U8, [c0], 15, periodic=0), gol_cube_numpy(c0, 15))
+
+
+def test_gol_8192_config_against_oracle_100_steps():
+    with lgd.Grid(lgd.CELL_GOL_U8, (8192, 8192), periodic=3) as g:
+        g.fill_bernoulli(0.3, seed=42, stream=workloads.STREAM_GRID)
+        c0 = g.download(0)
+        np.testing.assert_array_equal(c0[:4], workloads.gol_initial(8192, 8192, seed=42)[:4])
+        g.step(100)
+        out = g.download(0)
+    np.testing.assert_array_equal(out, oracle.gol(c0, 100))
+
+
+# ------------------------------------------------------------- var-coef
+def test_varcoef_f64_bit_exact():
+    g = load("varcoef_16")
+    out = run_grid(lgd.CELL_VARCOEF_F64, [g["u0"], g["k"]], int(g["steps"]), periodic=7)
+    np.testing.assert_array_equal(out, g["out"])
+
+
+def test_varcoef_f32_error_against_fp64():
+    u0, k = workloads.varcoef_fields(32, seed=42, length=8.0)
+    out = run_grid(lgd.CELL_VARCOEF_F32, [u0.astype(np.float32), k.astype(np.float32)], 64, periodic=7)
+    ref = oracle.varcoef(u0, k, 64)
+    rel_l2 = np.linalg.norm(out.astype(np.float64) - ref) / np.linalg.norm(ref)
+    assert rel_l2 < 1e-6, rel_l2
