@@ -1,25 +1,29 @@
 #!/usr/bin/env python3
 """Benchmark of the cell-update hot path (one JSON line on stdout).
 
-Workload (default): Jacobi-7 heat diffusion on a 512^3 grid of FP64 cells,
+Default workload: Jacobi-7 heat diffusion on a 512^3 grid of FP64 cells,
 constant zero boundary, U[0,1) initial values (seeded SplitMix64) - the
 grid the Jacobi3D GLUPS target is quoted on.  A "step" is one time step of
-the whole grid (134,217,728 lattice-site updates).  The grid (1 GiB per
-buffer) is larger than L2, so consecutive steps read from HBM.
+the whole grid (134,217,728 lattice-site updates, one kernel launch).  The
+grid (1 GiB per buffer) is larger than L2, so every step streams from HBM.
 
   value  GLUPS with the grid resident in HBM, timed with CUDA events on the
          library's stream over exactly --steps launches.
-  e2e    GLUPS through the C ABI with host buffers: upload from pinned host
-         memory, 100 time steps (the run length of the configuration), and
-         download of the result, per e2e step.
+  e2e    the same metric through the C ABI with host buffers: upload from
+         pinned host memory, the configuration's run length of time steps,
+         download of the result - per e2e step.
+
+Other workloads (--workload): gol_u8_8192 (Game of Life 8192^2 torus),
+sell_f64_4m (SELL-C-sigma diffusion, 4,194,304 nodes, C=32, sigma=256),
+jacobi7_f64_ieee_512 (the bit-exact IEEE FP64 kernel alone).
 
 --impl reference times the reference's CPU algorithm on this machine's host
-cores instead: the C restatement in oracle/ (the reference itself cannot be
-built here), OpenMP over all cores, on whole time steps of the same grid.
+cores: the C restatement in oracle/ (the reference itself is not built on
+this machine), OpenMP over all cores, on whole time steps of the same input.
 
 Under torchrun (--gpus N > 1) every rank advances its own replica (the
-workload is replicated, not sharded: weak scaling with no collective on the
-data path); rank 0 prints the line with the max time over ranks.
+workload is replicated, not sharded: weak scaling, no collective on the data
+path); rank 0 prints the line with the max time over ranks.
 """
 from __future__ import annotations
 
@@ -37,12 +41,7 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-WORKLOADS = {
-    # name: (cell, shape, periodic, steps per e2e run, bytes per LUP)
-    "jacobi7_f64_512": ("fix", (512, 512, 512), 0, 100, 16),
-    "jacobi7_f64_ieee_512": ("ieee", (512, 512, 512), 0, 100, 16),
-    "gol_u8_8192": ("gol", (8192, 8192), 3, 1000, 2),
-}
+JACOBI_METRIC = "Jacobi3D GLUPS & HBM GB/s vs 8 TB/s"
 
 
 def load_peaks():
@@ -55,15 +54,14 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel_key: str):
+def profile_traffic(key: str):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (profiles/ncu_traffic.txt: lines 'key bytes_per_launch')."""
-    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    summary (profiles/ncu_traffic.txt, lines 'workload bytes_per_launch')."""
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.txt")) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) >= 2 and parts[0] == kernel_key:
+                if len(parts) >= 2 and parts[0] == key:
                     return float(parts[1])
     except OSError:
         pass
@@ -89,6 +87,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
                  "-lms", "100", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
         except Exception:
             self.proc = None
         return self
@@ -126,7 +125,164 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def dist_setup(n_gpus: int):
+# ---------------------------------------------------------------- workloads
+class JacobiWorkload:
+    shape = (512, 512, 512)
+    run_steps = 100
+    bytes_per_unit = 16          # one FP64 read + one FP64 write per cell and step
+
+    def __init__(self, ieee: bool):
+        from libgeodecomp_gb300 import lgd, workloads
+        self.lgd = lgd
+        self.ieee = ieee
+        self.name = "jacobi7_f64_ieee_512" if ieee else "jacobi7_f64_512"
+        self.metric = JACOBI_METRIC
+        self.unit = "GLUPS"
+        self.units = int(np.prod(self.shape))
+        self.dtype = "f64" if ieee else "f64 (values on the device in 64-bit fixed point, integer arithmetic)"
+        cell = lgd.CELL_JACOBI7_F64 if ieee else lgd.CELL_JACOBI7_F64_FIX
+        self.g = lgd.Grid(cell, self.shape, periodic=0)
+        self.g.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
+        self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "constant 0",
+                       "cells": self.units, "l2": "inputs larger than L2 (1 GiB per buffer)",
+                       "cell_update": "(c+n+s+e+w+t+b)*(1/7)"}
+
+    def stream(self):
+        p = self.lgd.ctypes.c_void_p()
+        self.lgd.check(self.lgd.lib().lgd_gpu_stream(self.g._h, self.lgd.ctypes.byref(p)))
+        return p.value
+
+    def step(self, n=1):
+        self.g.step(n)
+
+    def sync(self):
+        self.g.synchronize()
+
+    def launches(self):
+        return self.g.launch_count()
+
+    def host_buffers(self, torch):
+        nbytes = self.units * 8
+        hin = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64).reshape(self.shape)
+        hout = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64).reshape(self.shape)
+        self.g.download(0, out=hin)
+        return hin, hout
+
+    def e2e_run(self, hin, hout):
+        self.g.upload(0, hin)
+        self.g.step(self.run_steps)
+        self.g.download(0, out=hout)
+        return hin.nbytes, hout.nbytes
+
+    def close(self):
+        self.g.close()
+
+
+class GoLWorkload:
+    shape = (8192, 8192)
+    run_steps = 1000
+    bytes_per_unit = 2
+
+    def __init__(self):
+        from libgeodecomp_gb300 import lgd, workloads
+        self.lgd = lgd
+        self.name = "gol_u8_8192"
+        self.metric = "Game of Life GLUPS"
+        self.unit = "GLUPS"
+        self.units = int(np.prod(self.shape))
+        self.dtype = "u8"
+        self.g = lgd.Grid(lgd.CELL_GOL_U8, self.shape, periodic=3)
+        self.g.fill_bernoulli(0.3, seed=42, stream=workloads.STREAM_GRID)
+        self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "torus", "cells": self.units,
+                       "l2": "both buffers (128 MiB) about L2-sized; no flush between steps"}
+
+    stream = JacobiWorkload.stream
+    step = JacobiWorkload.step
+    sync = JacobiWorkload.sync
+    launches = JacobiWorkload.launches
+    e2e_run = JacobiWorkload.e2e_run
+    close = JacobiWorkload.close
+
+    def host_buffers(self, torch):
+        hin = torch.empty(self.units, dtype=torch.uint8, pin_memory=True).numpy().reshape(self.shape)
+        hout = torch.empty(self.units, dtype=torch.uint8, pin_memory=True).numpy().reshape(self.shape)
+        self.g.download(0, out=hin)
+        return hin, hout
+
+
+class SellWorkload:
+    n = 4194304
+    run_steps = 200
+
+    def __init__(self):
+        from libgeodecomp_gb300 import lgd, workloads
+        self.lgd = lgd
+        self.name = "sell_f64_4m"
+        self.metric = "SELL-C-sigma diffusion GB/s and s/step"
+        self.unit = "GLUPS"
+        rp, col, w = workloads.powerlaw_graph(self.n, seed=42)
+        self.nnz = int(col.size)
+        self.s = lgd.sell_build(self.n, rp, col, w, 32, 256)
+        self.x0 = workloads.sell_values(self.n, seed=42)
+        self.g = lgd.SellGrid(self.s)
+        self.g.upload(self.x0)
+        self.units = self.n
+        n_chunks = (self.n - 1) // 32 + 1
+        # 12 B per stored entry (8 value + 4 column), 16 B per row (x own read
+        # + x' write) + 4 B row length, 4 B per chunk offset
+        self.bytes_per_step = 12 * self.nnz + 20 * self.n + 4 * n_chunks
+        self.bytes_per_unit = self.bytes_per_step / self.n
+        self.dtype = "f64"
+        self.config = {"workload": self.name, "nodes": self.n, "nnz": self.nnz,
+                       "slots": int(self.s["values"].size), "C": 32, "sigma": 256,
+                       "degree": "power law alpha=2 on [4,64]",
+                       "l2": "matrix (%d MiB) larger than L2; x (32 MiB) L2-resident" % (12 * self.nnz >> 20)}
+
+    def stream(self):
+        return self.g.stream()
+
+    def step(self, n=1):
+        self.g.step(n)
+
+    def sync(self):
+        self.g.synchronize()
+
+    def launches(self):
+        return self.g.launch_count()
+
+    def host_buffers(self, torch):
+        hin = torch.empty(self.n * 8, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64)
+        hout = torch.empty(self.n * 8, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64)
+        hin[:] = self.x0
+        return hin, hout
+
+    def e2e_run(self, hin, hout):
+        self.g.upload(hin)
+        self.g.step(self.run_steps)
+        self.g.download(out=hout)
+        return hin.nbytes, hout.nbytes
+
+    def close(self):
+        self.g.close()
+
+
+def make_workload(name):
+    if name == "jacobi7_f64_512":
+        return JacobiWorkload(ieee=False)
+    if name == "jacobi7_f64_ieee_512":
+        return JacobiWorkload(ieee=True)
+    if name == "gol_u8_8192":
+        return GoLWorkload()
+    if name == "sell_f64_4m":
+        return SellWorkload()
+    raise ValueError(name)
+
+
+WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "gol_u8_8192", "sell_f64_4m"]
+
+
+# ------------------------------------------------------------------ helpers
+def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -151,108 +307,83 @@ def max_over_ranks(dist, v: float) -> float:
     return float(t.item())
 
 
+def time_steps(torch, w, steps):
+    stream = torch.cuda.ExternalStream(w.stream())
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        w.step(1)
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end)
+
+
 def run_gpu(args, world, rank, local, dist):
     import torch
     torch.cuda.set_device(local)
-    from libgeodecomp_gb300 import lgd, workloads
-
-    kind, shape, periodic, run_steps, bpl = WORKLOADS[args.workload]
-    cell = {"fix": lgd.CELL_JACOBI7_F64_FIX, "ieee": lgd.CELL_JACOBI7_F64, "gol": lgd.CELL_GOL_U8}[kind]
-    cells = int(np.prod(shape))
-    g = lgd.Grid(cell, shape, periodic=periodic)
-    if kind == "gol":
-        g.fill_bernoulli(0.3, seed=42, stream=workloads.STREAM_GRID)
-    else:
-        g.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
-    stream_ptr = lgd.ctypes.c_void_p()
-    lgd.check(lgd.lib().lgd_gpu_stream(g._h, lgd.ctypes.byref(stream_ptr)))
-    stream = torch.cuda.ExternalStream(stream_ptr.value)
-
+    w = make_workload(args.workload)
     for _ in range(args.warmup):
-        g.step(1)
-    g.synchronize()
-    launches0 = g.launch_count()
-    start = torch.cuda.Event(enable_timing=True)
-    end = torch.cuda.Event(enable_timing=True)
+        w.step(1)
+    w.sync()
+    launches0 = w.launches()
     barrier(dist)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        start.record(stream)
-        for _ in range(args.steps):
-            g.step(1)
-        end.record(stream)
-        end.synchronize()
+        ms = time_steps(torch, w, args.steps)
     torch.cuda.synchronize()
     barrier(dist)
-    ms = start.elapsed_time(end)
-    launches = g.launch_count() - launches0
+    launches = w.launches() - launches0
     ms = max_over_ranks(dist, ms)
     clocks = clk.summary()
     ms_per_step = ms / args.steps
-    glups = cells * args.steps * world / (ms * 1e-3) / 1e9
+    value = w.units * args.steps * world / (ms * 1e-3) / 1e9
 
-    # roofline of the dominant kernel (one launch per step)
     peak, peak_kind = load_peaks()
-    achieved = cells * bpl / (ms_per_step * 1e-3) / 1e9
+    algo_bytes = w.units * w.bytes_per_unit
+    achieved = algo_bytes / (ms_per_step * 1e-3) / 1e9
+    traffic = profile_traffic(w.name)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": cells * bpl,
-                "traffic": profile_traffic(args.workload)}
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": int(algo_bytes), "launch_ms": round(ms_per_step, 4),
+                "traffic": traffic}
 
-    # end to end through the C ABI: pinned host in, run_steps steps, host out
     e2e = None
     if not args.no_e2e:
-        host_dtype = np.uint8 if kind == "gol" else np.float64
-        hin = torch.empty(cells * np.dtype(host_dtype).itemsize, dtype=torch.uint8, pin_memory=True).numpy()
-        hout = torch.empty(cells * np.dtype(host_dtype).itemsize, dtype=torch.uint8, pin_memory=True).numpy()
-        hin_v = hin.view(host_dtype).reshape(shape)
-        hout_v = hout.view(host_dtype).reshape(shape)
-        g.download(0, out=hin_v)
-        e2e_runs = max(1, args.e2e_runs)
-        # warm-up run
-        g.upload(0, hin_v)
-        g.step(run_steps)
-        g.download(0, out=hout_v)
+        hin, hout = w.host_buffers(torch)
+        w.e2e_run(hin, hout)     # warm-up
+        runs = max(1, args.e2e_runs)
         barrier(dist)
         t0 = time.perf_counter()
-        for _ in range(e2e_runs):
-            g.upload(0, hin_v)
-            g.step(run_steps)
-            g.download(0, out=hout_v)
+        for _ in range(runs):
+            bi, bo = w.e2e_run(hin, hout)
         t1 = time.perf_counter()
         barrier(dist)
         e2e_s = max_over_ranks(dist, t1 - t0)
-        e2e = {"value": round(cells * run_steps * e2e_runs * world / e2e_s / 1e9, 3), "unit": "GLUPS",
-               "h2d_bytes_per_step": cells * np.dtype(host_dtype).itemsize,
-               "d2h_bytes_per_step": cells * np.dtype(host_dtype).itemsize,
-               "step": "upload + %d time steps + download via the C ABI" % run_steps,
-               "ms_per_step": round(e2e_s * 1e3 / e2e_runs, 3)}
+        e2e = {"value": round(w.units * w.run_steps * runs * world / e2e_s / 1e9, 3), "unit": w.unit,
+               "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
+               "step": "upload from pinned host + %d time steps + download, through the C ABI" % w.run_steps,
+               "ms_per_step": round(e2e_s * 1e3 / runs, 3)}
 
     extra = {}
     if args.workload == "jacobi7_f64_512" and not args.no_ieee:
-        # the bit-exact IEEE FP64 kernel on the same grid, for comparison
-        gi = lgd.Grid(lgd.CELL_JACOBI7_F64, shape, periodic=periodic)
-        gi.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
-        sp = lgd.ctypes.c_void_p()
-        lgd.check(lgd.lib().lgd_gpu_stream(gi._h, lgd.ctypes.byref(sp)))
-        st = torch.cuda.ExternalStream(sp.value)
+        w.close()
+        wi = make_workload("jacobi7_f64_ieee_512")
         for _ in range(3):
-            gi.step(1)
-        gi.synchronize()
+            wi.step(1)
+        wi.sync()
         k = max(3, args.steps // 4)
-        s0 = torch.cuda.Event(enable_timing=True)
-        s1 = torch.cuda.Event(enable_timing=True)
-        s0.record(st)
-        for _ in range(k):
-            gi.step(1)
-        s1.record(st)
-        s1.synchronize()
-        ims = s0.elapsed_time(s1) / k
-        extra["ieee_fp64_kernel"] = {"glups": round(cells / (ims * 1e-3) / 1e9, 2), "ms_per_step": round(ims, 4),
-                                     "hbm_frac": round(cells * 16 / (ims * 1e-3) / 1e9 / peak, 4),
-                                     "note": "bit-identical to the reference; bound by the FP64 pipe"}
-        gi.close()
-    g.close()
+        ims = time_steps(torch, wi, k) / k
+        extra["ieee_fp64_kernel"] = {
+            "glups": round(wi.units / (ims * 1e-3) / 1e9, 2), "ms_per_step": round(ims, 4),
+            "hbm_frac": round(wi.units * 16 / (ims * 1e-3) / 1e9 / peak, 4),
+            "note": "LGD_CELL_JACOBI7_F64: bit-identical to the reference; bound by the GPU's FP64 rate"}
+        wi.close()
+    else:
+        w.close()
+    if args.workload == "sell_f64_4m":
+        extra["s_per_step"] = round(ms_per_step * 1e-3, 7)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -260,15 +391,11 @@ def run_gpu(args, world, rank, local, dist):
 
     if rank == 0:
         line = {
-            "metric": "Jacobi3D GLUPS & HBM GB/s vs 8 TB/s" if kind != "gol" else "Game of Life GLUPS",
-            "value": round(glups, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
+            "metric": w.metric, "value": round(value, 3), "unit": w.unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fix": "f64 (64-bit fixed-point arithmetic)", "ieee": "f64", "gol": "u8"}[kind],
-            "data": "synthetic (seeded SplitMix64 U[0,1), generated on device)",
-            "config": {"workload": args.workload, "grid": list(shape), "boundary": "constant 0" if periodic == 0 else "torus",
-                       "cells": cells, "l2": "grid (%d MiB per buffer) larger than L2" % (cells * bpl // 2 >> 20),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "scaling": "weak", "vs_baseline": None, "dtype": w.dtype,
+            "data": "synthetic (seeded SplitMix64, generated on device or by libgeodecomp_gb300.workloads)",
+            "config": dict(w.config, parallelism="replicas" if world > 1 else "single GPU"),
             "gpu_launches": launches, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
         }
         line.update(extra)
@@ -277,63 +404,66 @@ def run_gpu(args, world, rank, local, dist):
         dist.destroy_process_group()
 
 
-def cpu_baseline(workload: str, budget_s: float = 15.0):
-    """The oracle (C restatement of the reference algorithm) on all host
-    cores, timed on whole time steps of the same grid until about budget_s
-    seconds of work."""
+# ------------------------------------------------------------ CPU baseline
+def cpu_stepper(name):
+    """(units per step, function advancing the input by s steps) of the
+    oracle for a workload."""
     import oracle
     from libgeodecomp_gb300 import workloads
-    kind, shape, periodic, _, _ = WORKLOADS[workload]
-    threads = oracle.max_threads()
-    cells = int(np.prod(shape))
-    if kind == "gol":
-        u = workloads.gol_initial(shape[1], shape[0], seed=42)
-        fn = lambda a, s: oracle.gol(a, s)  # noqa: E731
-    else:
-        u = workloads.jacobi_initial(shape[2], shape[1], shape[0], seed=42)
-        fn = lambda a, s: oracle.jacobi7(a, s)  # noqa: E731
-    fn(u, 1)
+    if name.startswith("jacobi7"):
+        u = workloads.jacobi_initial(512, 512, 512, seed=42)
+        return u.size, u, lambda a, s: oracle.jacobi7(a, s)
+    if name == "gol_u8_8192":
+        c = workloads.gol_initial(8192, 8192, seed=42)
+        return c.size, c, lambda a, s: oracle.gol(a, s)
+    if name == "sell_f64_4m":
+        n = 4194304
+        rp, col, w = workloads.powerlaw_graph(n, seed=42)
+        s = oracle.sell_build(n, rp, col, w, 32, 256)
+        x = workloads.sell_values(n, seed=42)[s["perm"]]
+        return n, x, lambda a, k: oracle.sell_diffusion(s, 32, a, k)
+    raise ValueError(name)
+
+
+def cpu_baseline(name: str, budget_s: float = 15.0):
+    """The oracle on all host cores, on whole time steps of the same input,
+    for about budget_s seconds."""
+    import oracle
+    units, state, fn = cpu_stepper(name)
+    fn(state, 1)
     t0 = time.perf_counter()
-    fn(u, 1)
+    fn(state, 1)
     one = time.perf_counter() - t0
     steps = max(1, int(budget_s / max(one, 1e-6)))
     t0 = time.perf_counter()
-    fn(u, steps)
+    fn(state, steps)
     dt = time.perf_counter() - t0
-    return {"value": round(cells * steps / dt / 1e9, 4), "unit": "GLUPS", "cores": threads, "kind": "port",
-            "sample": "%d time steps of the %s grid (%.1f s)" % (steps, "x".join(map(str, shape)), dt)}
+    return {"value": round(units * steps / dt / 1e9, 4), "unit": "GLUPS", "cores": oracle.max_threads(),
+            "kind": "port", "sample": "%d whole time steps of the %s input (%.1f s)" % (steps, name, dt)}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    from libgeodecomp_gb300 import workloads  # noqa: F401
     import oracle
-    kind, shape, periodic, _, _ = WORKLOADS[args.workload]
-    cells = int(np.prod(shape))
-    if kind == "gol":
-        u = workloads.gol_initial(shape[1], shape[0], seed=42)
-        fn = lambda a, s: oracle.gol(a, s)  # noqa: E731
-    else:
-        u = workloads.jacobi_initial(shape[2], shape[1], shape[0], seed=42)
-        fn = lambda a, s: oracle.jacobi7(a, s)  # noqa: E731
+    units, state, fn = cpu_stepper(args.workload)
     for _ in range(args.warmup):
-        u = fn(u, 1)
+        state = fn(state, 1)
     t0 = time.perf_counter()
-    u = fn(u, args.steps)
+    state = fn(state, args.steps)
     dt = time.perf_counter() - t0
-    glups = cells * args.steps / dt / 1e9
-    threads = oracle.max_threads()
+    value = units * args.steps / dt / 1e9
+    w_metric = JACOBI_METRIC if args.workload.startswith("jacobi7") else (
+        "Game of Life GLUPS" if args.workload == "gol_u8_8192" else "SELL-C-sigma diffusion GB/s and s/step")
     line = {
-        "metric": "Jacobi3D GLUPS & HBM GB/s vs 8 TB/s" if kind != "gol" else "Game of Life GLUPS",
-        "value": round(glups, 4), "unit": "GLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if kind != "gol" else "u8", "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": args.workload, "grid": list(shape), "cells": cells},
+        "metric": w_metric, "value": round(value, 4), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8" if args.workload == "gol_u8_8192" else "f64",
+        "data": "synthetic (seeded SplitMix64)", "config": {"workload": args.workload},
         "impl": "reference",
-        "cpu_baseline": {"value": round(glups, 4), "unit": "GLUPS", "cores": threads, "kind": "port",
-                         "sample": "%d whole time steps of the %s grid" % (args.steps, "x".join(map(str, shape)))},
-        "e2e": {"value": round(glups, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": oracle.max_threads(), "kind": "port",
+                         "sample": "%d whole time steps of the %s input" % (args.steps, args.workload)},
+        "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -344,7 +474,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="jacobi7_f64_512")
+    ap.add_argument("--workload", choices=WORKLOAD_NAMES, default="jacobi7_f64_512")
     ap.add_argument("--e2e-runs", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
@@ -356,7 +486,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
-    world, rank, local, dist = dist_setup(args.gpus)
+    world, rank, local, dist = dist_setup()
     run_gpu(args, world, rank, local, dist)
 
 

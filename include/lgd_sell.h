@@ -1,0 +1,86 @@
+/*
+ * lgd_sell.h - C ABI for unstructured grids stored as SELL-C-sigma.
+ *
+ * Builder (host): lays out a sparse adjacency matrix exactly as the
+ * reference's ReorderingUnstructuredGrid + SellCSigmaSparseMatrixContainer
+ * do, so the arrays can be compared byte for byte or handed over.
+ * Device (one handle): the diffusion cell x' = 0.1 x + W x on the
+ * physical (sigma-sorted) order, double-buffered.
+ *
+ * Status codes and lgd_gpu_last_error() are shared with lgd_gpu.h.
+ */
+#ifndef LGD_SELL_H
+#define LGD_SELL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "lgd_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Row order and chunk geometry.  Input: CSR row_ptr[n+1] of the logical
+ * matrix.  Output: perm[n] (physical row p holds logical row perm[p]),
+ * row_length[rows_padded], chunk_length[n_chunks], chunk_offset[n_chunks+1]
+ * with n_chunks = (n-1)/C + 1, rows_padded = n_chunks*C, and *total value
+ * slots.  Replaces the sigma-window sort of ReorderingUnstructuredGrid::
+ * setWeights (storage/reorderingunstructuredgrid.h:195-252) and the
+ * chunk-length/offset pass of InitFromMatrix
+ * (storage/sellcsigmasparsematrixcontainer.h:82-127). */
+int lgd_sell_plan(int n, const int64_t *row_ptr, int C, int sigma, int32_t *perm, int32_t *row_length,
+                  int32_t *chunk_length, int32_t *chunk_offset, int64_t *total);
+
+/* Values and columns (total slots each).  remap_columns = 1: column ids
+ * become physical ids (the grid path, storage/reorderingunstructuredgrid.
+ * h:254-283); 0: logical ids kept (the bare container).  Replaces
+ * InitFromMatrix's value placement (storage/sellcsigmasparsematrixcontainer.
+ * h:129-160). */
+int lgd_sell_fill(int n, const int64_t *row_ptr, const int32_t *col, const double *w, int C, const int32_t *perm,
+                  const int32_t *chunk_offset, int64_t total, int remap_columns, double *values, int32_t *column);
+
+typedef struct lgd_sell lgd_sell;
+
+/* flags */
+#define LGD_SELL_EXACT 1   /* separate multiply and add (bit-identical to the
+                              reference build); default fuses them (FMA) */
+
+/* Uploads the SELL arrays (chunk_offset[n_chunks+1], row_length
+ * [rows_padded], values/column[total] with physical column ids) and
+ * allocates the double-buffered node vector.  precision: 8 = FP64, 4 = FP32
+ * (values and node values rounded to float).  perm (may be NULL) enables
+ * logical-order uploads/downloads.  Replaces the device side of an
+ * UnstructuredSoAGrid with its SellCSigmaSparseMatrixContainer
+ * (storage/unstructuredsoagrid.h:35-101). */
+int lgd_sell_create(int n, int C, int64_t total, const int32_t *chunk_offset, const int32_t *row_length,
+                    const double *values, const int32_t *column, const int32_t *perm, int precision, int flags,
+                    lgd_sell **out);
+int lgd_sell_destroy(lgd_sell *h);
+
+/* Node values (n doubles), current (which = 0) or next (1) buffer;
+ * logical = 1 maps through perm (GridBase::get/set on a reordering grid,
+ * storage/reorderingunstructuredgrid.h:300-340), 0 uses physical order. */
+int lgd_sell_upload_x(lgd_sell *h, int which, int logical, const double *x, size_t bytes);
+int lgd_sell_download_x(lgd_sell *h, int which, int logical, double *x, size_t bytes);
+
+/* count time steps x <- 0.1 x + W x, swapping after each.  Replaces
+ * UnstructuredUpdateFunctor (storage/unstructuredupdatefunctor.h:121-229)
+ * driving the cell's updateLineX over the whole node set. */
+int lgd_sell_step(lgd_sell *h, int count);
+
+/* Updates physical rows [row_begin, row_end) into the next buffer, no swap
+ * (a one-streak region, including streaks that start or end inside a chunk:
+ * the reference peels those with unstructuredLoopPeeler,
+ * storage/unstructuredlooppeeler.h:75-126). */
+int lgd_sell_update_rows(lgd_sell *h, int row_begin, int row_end);
+int lgd_sell_swap(lgd_sell *h);
+int lgd_sell_synchronize(lgd_sell *h);
+int lgd_sell_stream(lgd_sell *h, void **stream);
+int lgd_sell_launch_count(lgd_sell *h, uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

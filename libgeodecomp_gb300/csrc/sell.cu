@@ -1,0 +1,467 @@
+// Unstructured grids in SELL-C-sigma form: the host-side builder and the
+// device diffusion step x' = 0.1 x + W x.
+//
+// Builder.  The layout is the reference's, byte for byte, so that grids
+// built by either side can be exchanged:
+//   - ReorderingUnstructuredGrid::setWeights (storage/
+//     reorderingunstructuredgrid.h:195-284): inside windows of sigma rows
+//     the rows are stably sorted by decreasing length; physical row p holds
+//     logical row perm[p]; column ids are remapped to physical ids;
+//   - SellCSigmaSparseMatrixContainer / InitFromMatrix (storage/
+//     sellcsigmasparsematrixcontainer.h:49-161): chunks of C rows,
+//     chunkLength = longest row of the chunk, chunkOffset[c+1] =
+//     chunkOffset[c] + C * chunkLength[c], entry k of row r at
+//     chunkOffset[r / C] + k * C + r % C, a row's entries in ascending
+//     (physical) column order, padding value 0 / column 0.
+// The window sort here is a counting sort on the row length (stable by
+// construction), the per-row column sort an insertion sort (rows are short).
+//
+// Kernel.  C = 32 puts one chunk on one warp: lane l owns row
+// chunk * 32 + l, entry k of all 32 rows is one coalesced 256-byte load of
+// values and a 128-byte load of columns, and the x[column] gathers hit L2
+// (the FP64 vector of 4M nodes is 32 MiB).  Other C values use one thread
+// per row with the same indexing.  Each lane stops at its own row length,
+// as the reference's neighbourhood iterator does
+// (storage/unstructuredneighborhood.h:154-170), so padding costs no traffic.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "lgd_internal.h"
+#include "../../include/lgd_sell.h"
+
+namespace lgd {
+
+struct Sell {
+    int n;                  // rows (nodes)
+    int C;
+    int n_chunks;
+    int rows_padded;
+    long long total;        // value slots
+    int precision;          // 8 (FP64) or 4 (FP32)
+    int flags;
+    int *d_chunk_offset;    // n_chunks + 1
+    int *d_row_length;      // rows_padded
+    void *d_values;         // total, FP64 or FP32
+    int *d_column;          // total
+    void *d_x[2];           // rows_padded each
+    int *d_perm;            // physical -> logical (n), or null
+    int cur;
+    cudaStream_t stream;
+    uint64_t launches;
+};
+
+// -------------------------------------------------------------- kernels
+template<typename R, bool EXACT>
+__device__ __forceinline__ R madd(R acc, R a, R b);
+
+template<>
+__device__ __forceinline__ double madd<double, true>(double acc, double a, double b)
+{
+    return __dadd_rn(acc, __dmul_rn(a, b));
+}
+
+template<>
+__device__ __forceinline__ double madd<double, false>(double acc, double a, double b)
+{
+    return fma(a, b, acc);
+}
+
+template<>
+__device__ __forceinline__ float madd<float, false>(float acc, float a, float b)
+{
+    return fmaf(a, b, acc);
+}
+
+template<>
+__device__ __forceinline__ float madd<float, true>(float acc, float a, float b)
+{
+    return __fadd_rn(acc, __fmul_rn(a, b));
+}
+
+// one thread per row; row = blockIdx * blockDim + thread, so a warp of 32
+// consecutive rows is one chunk when C = 32
+template<typename R, bool EXACT>
+__global__ void __launch_bounds__(256)
+sell_diffusion_kernel(const int *__restrict__ chunk_offset, const int *__restrict__ row_length,
+                      const R *__restrict__ values, const int *__restrict__ column,
+                      const R *__restrict__ x, R *__restrict__ xn, int n, int C, int row_begin, int row_end)
+{
+    const int row = row_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= row_end) return;
+    const int chunk = row / C;
+    const long long base = (long long)chunk_offset[chunk] + (row - chunk * C);
+    const int len = row_length[row];
+    R acc = (R)0;
+    const R *v = values + base;
+    const int *c = column + base;
+    int k = 0;
+    // two independent gathers in flight per iteration
+    for (; k + 1 < len; k += 2) {
+        const R w0 = __ldg(v + (long long)k * C);
+        const int c0 = __ldg(c + (long long)k * C);
+        const R w1 = __ldg(v + (long long)(k + 1) * C);
+        const int c1 = __ldg(c + (long long)(k + 1) * C);
+        const R x0 = __ldg(x + c0);
+        const R x1 = __ldg(x + c1);
+        acc = madd<R, EXACT>(acc, x0, w0);
+        acc = madd<R, EXACT>(acc, x1, w1);
+    }
+    if (k < len) {
+        const R w0 = __ldg(v + (long long)k * C);
+        const int c0 = __ldg(c + (long long)k * C);
+        acc = madd<R, EXACT>(acc, __ldg(x + c0), w0);
+    }
+    // x' = 0.1 * x + acc
+    if (EXACT) {
+        xn[row] = (sizeof(R) == 8) ? (R)__dadd_rn(__dmul_rn(0.1, (double)x[row]), (double)acc)
+                                   : (R)__fadd_rn(__fmul_rn(0.1f, (float)x[row]), (float)acc);
+    } else {
+        xn[row] = (R)0.1 * x[row] + acc;
+    }
+}
+
+template<typename R>
+__global__ void permute_in_kernel(const double *logical, const int *perm, R *phys, int n)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        phys[p] = (R)logical[perm ? perm[p] : p];
+    }
+}
+
+template<typename R>
+__global__ void permute_out_kernel(const R *phys, const int *perm, double *logical, int n)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        logical[perm ? perm[p] : p] = (double)phys[p];
+    }
+}
+
+static Sell& sell_of(lgd_sell *h)
+{
+    LGD_REQUIRE(h != nullptr, LGD_ERR_INVALID, "null handle");
+    return *reinterpret_cast<Sell *>(h);
+}
+
+static void sell_free(Sell& s)
+{
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    cudaFree(s.d_chunk_offset);
+    cudaFree(s.d_row_length);
+    cudaFree(s.d_values);
+    cudaFree(s.d_column);
+    cudaFree(s.d_x[0]);
+    cudaFree(s.d_x[1]);
+    cudaFree(s.d_perm);
+    if (s.stream) cudaStreamDestroy(s.stream);
+}
+
+static void launch_sell(Sell& s, int row_begin, int row_end)
+{
+    if (row_end <= row_begin) return;
+    const int threads = 256;
+    const int blocks = (row_end - row_begin + threads - 1) / threads;
+    const bool exact = (s.flags & LGD_SELL_EXACT) != 0;
+    if (s.precision == 8) {
+        const double *x = (const double *)s.d_x[s.cur];
+        double *xn = (double *)s.d_x[1 - s.cur];
+        if (exact) {
+            sell_diffusion_kernel<double, true><<<blocks, threads, 0, s.stream>>>(
+                s.d_chunk_offset, s.d_row_length, (const double *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        } else {
+            sell_diffusion_kernel<double, false><<<blocks, threads, 0, s.stream>>>(
+                s.d_chunk_offset, s.d_row_length, (const double *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        }
+    } else {
+        const float *x = (const float *)s.d_x[s.cur];
+        float *xn = (float *)s.d_x[1 - s.cur];
+        if (exact) {
+            sell_diffusion_kernel<float, true><<<blocks, threads, 0, s.stream>>>(
+                s.d_chunk_offset, s.d_row_length, (const float *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        } else {
+            sell_diffusion_kernel<float, false><<<blocks, threads, 0, s.stream>>>(
+                s.d_chunk_offset, s.d_row_length, (const float *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        }
+    }
+    check_launch("sell diffusion");
+    ++s.launches;
+}
+
+}  // namespace lgd
+
+using namespace lgd;
+
+extern "C" {
+
+int lgd_sell_plan(int n, const int64_t *row_ptr, int C, int sigma, int32_t *perm, int32_t *row_length,
+                  int32_t *chunk_length, int32_t *chunk_offset, int64_t *total)
+{
+    return guard([&] {
+        LGD_REQUIRE(n > 0, LGD_ERR_INVALID, "node count must be positive");
+        LGD_REQUIRE(C >= 1 && sigma >= 1, LGD_ERR_INVALID, "C and sigma must be at least 1");
+        LGD_REQUIRE(row_ptr && perm && row_length && chunk_length && chunk_offset && total, LGD_ERR_INVALID,
+                    "null argument");
+        LGD_REQUIRE(row_ptr[0] == 0, LGD_ERR_INVALID, "row_ptr[0] must be 0");
+        int max_len = 0;
+        for (int r = 0; r < n; ++r) {
+            const long long d = row_ptr[r + 1] - row_ptr[r];
+            LGD_REQUIRE(d >= 0 && d <= (1 << 30), LGD_ERR_INVALID, "row_ptr must be non-decreasing");
+            max_len = std::max(max_len, (int)d);
+        }
+        // stable counting sort by decreasing length inside each window
+        std::vector<int> count(max_len + 2);
+        for (int w0 = 0; w0 < n; w0 += sigma) {
+            const int cnt = std::min(sigma, n - w0);
+            std::fill(count.begin(), count.end(), 0);
+            for (int i = 0; i < cnt; ++i) {
+                const int d = (int)(row_ptr[w0 + i + 1] - row_ptr[w0 + i]);
+                ++count[max_len - d + 1];
+            }
+            for (int b = 1; b < (int)count.size(); ++b) count[b] += count[b - 1];
+            for (int i = 0; i < cnt; ++i) {
+                const int d = (int)(row_ptr[w0 + i + 1] - row_ptr[w0 + i]);
+                perm[w0 + count[max_len - d]++] = w0 + i;
+            }
+        }
+        const int n_chunks = (n - 1) / C + 1;
+        const int rows_padded = n_chunks * C;
+        for (int p = 0; p < rows_padded; ++p) {
+            row_length[p] = (p < n) ? (int)(row_ptr[perm[p] + 1] - row_ptr[perm[p]]) : 0;
+        }
+        long long acc = 0;
+        for (int c = 0; c < n_chunks; ++c) {
+            int m = 0;
+            for (int l = 0; l < C; ++l) m = std::max(m, row_length[c * C + l]);
+            chunk_length[c] = m;
+            LGD_REQUIRE(acc <= 0x7fffffffLL, LGD_ERR_RANGE, "more than 2^31-1 SELL value slots");
+            chunk_offset[c] = (int)acc;
+            acc += (long long)m * C;
+        }
+        LGD_REQUIRE(acc <= 0x7fffffffLL, LGD_ERR_RANGE, "more than 2^31-1 SELL value slots");
+        chunk_offset[n_chunks] = (int)acc;
+        *total = acc;
+    });
+}
+
+int lgd_sell_fill(int n, const int64_t *row_ptr, const int32_t *col, const double *w, int C, const int32_t *perm,
+                  const int32_t *chunk_offset, int64_t total, int remap_columns, double *values, int32_t *column)
+{
+    return guard([&] {
+        LGD_REQUIRE(n > 0 && C >= 1, LGD_ERR_INVALID, "bad sizes");
+        LGD_REQUIRE(row_ptr && perm && chunk_offset && (total == 0 || (values && column)), LGD_ERR_INVALID,
+                    "null argument");
+        LGD_REQUIRE(row_ptr[n] == 0 || (col && w), LGD_ERR_INVALID, "null matrix arrays");
+        std::vector<int> log_to_phys(n, -1);
+        for (int p = 0; p < n; ++p) {
+            LGD_REQUIRE(perm[p] >= 0 && perm[p] < n && log_to_phys[perm[p]] < 0, LGD_ERR_INVALID,
+                        "perm is not a permutation");
+            log_to_phys[perm[p]] = p;
+        }
+        std::memset(values, 0, sizeof(double) * (size_t)total);
+        std::memset(column, 0, sizeof(int32_t) * (size_t)total);
+        std::vector<std::pair<int, long long> > row;
+        for (int p = 0; p < n; ++p) {
+            const int r = perm[p];
+            const long long b = row_ptr[r];
+            const int d = (int)(row_ptr[r + 1] - b);
+            row.resize(d);
+            for (int k = 0; k < d; ++k) {
+                const int c = col[b + k];
+                LGD_REQUIRE(c >= 0 && c < n, LGD_ERR_RANGE, "column id outside the node set");
+                row[k] = std::make_pair(remap_columns ? log_to_phys[c] : c, b + k);
+            }
+            // insertion sort by column (ties keep input order)
+            for (int i = 1; i < d; ++i) {
+                std::pair<int, long long> t = row[i];
+                int j = i - 1;
+                while (j >= 0 && row[j].first > t.first) {
+                    row[j + 1] = row[j];
+                    --j;
+                }
+                row[j + 1] = t;
+            }
+            const long long base = (long long)chunk_offset[p / C] + p % C;
+            for (int k = 0; k < d; ++k) {
+                LGD_REQUIRE(base + (long long)k * C < total, LGD_ERR_INVALID, "chunk_offset does not fit the rows");
+                values[base + (long long)k * C] = w[row[k].second];
+                column[base + (long long)k * C] = row[k].first;
+            }
+        }
+    });
+}
+
+int lgd_sell_create(int n, int C, int64_t total, const int32_t *chunk_offset, const int32_t *row_length,
+                    const double *values, const int32_t *column, const int32_t *perm, int precision, int flags,
+                    lgd_sell **out)
+{
+    return guard([&] {
+        LGD_REQUIRE(out != nullptr, LGD_ERR_INVALID, "null output");
+        *out = nullptr;
+        LGD_REQUIRE(n > 0 && C >= 1 && total >= 0, LGD_ERR_INVALID, "bad sizes");
+        LGD_REQUIRE(precision == 8 || precision == 4, LGD_ERR_INVALID, "precision must be 8 (FP64) or 4 (FP32)");
+        LGD_REQUIRE(chunk_offset && row_length && (total == 0 || (values && column)), LGD_ERR_INVALID, "null argument");
+        const int n_chunks = (n - 1) / C + 1;
+        const int rows_padded = n_chunks * C;
+        LGD_REQUIRE(chunk_offset[0] == 0 && chunk_offset[n_chunks] == total, LGD_ERR_INVALID,
+                    "chunk_offset does not span the values");
+        for (int p = 0; p < rows_padded; ++p) {
+            const int c = p / C;
+            LGD_REQUIRE(row_length[p] >= 0 && (long long)row_length[p] * C <= chunk_offset[c + 1] - chunk_offset[c],
+                        LGD_ERR_INVALID, "row length exceeds its chunk");
+        }
+        for (long long i = 0; i < total; ++i) {
+            LGD_REQUIRE(column[i] >= 0 && column[i] < n, LGD_ERR_RANGE, "column id outside the node set");
+        }
+        Sell *s = new Sell();
+        std::memset(s, 0, sizeof(Sell));
+        s->n = n;
+        s->C = C;
+        s->n_chunks = n_chunks;
+        s->rows_padded = rows_padded;
+        s->total = total;
+        s->precision = precision;
+        s->flags = flags;
+        try {
+            LGD_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_chunk_offset, sizeof(int) * (n_chunks + 1)));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_row_length, sizeof(int) * rows_padded));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_values, (size_t)precision * std::max<long long>(total, 1)));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_column, sizeof(int) * std::max<long long>(total, 1)));
+            for (int b = 0; b < 2; ++b) {
+                LGD_CHECK_CUDA(cudaMalloc(&s->d_x[b], (size_t)precision * rows_padded));
+                LGD_CHECK_CUDA(cudaMemsetAsync(s->d_x[b], 0, (size_t)precision * rows_padded, s->stream));
+            }
+            LGD_CHECK_CUDA(cudaMemcpyAsync(s->d_chunk_offset, chunk_offset, sizeof(int) * (n_chunks + 1),
+                                           cudaMemcpyHostToDevice, s->stream));
+            LGD_CHECK_CUDA(cudaMemcpyAsync(s->d_row_length, row_length, sizeof(int) * rows_padded,
+                                           cudaMemcpyHostToDevice, s->stream));
+            if (total > 0) {
+                LGD_CHECK_CUDA(cudaMemcpyAsync(s->d_column, column, sizeof(int) * total, cudaMemcpyHostToDevice, s->stream));
+                if (precision == 8) {
+                    LGD_CHECK_CUDA(cudaMemcpyAsync(s->d_values, values, sizeof(double) * total, cudaMemcpyHostToDevice,
+                                                   s->stream));
+                } else {
+                    std::vector<float> vf(values, values + total);
+                    LGD_CHECK_CUDA(cudaMemcpyAsync(s->d_values, vf.data(), sizeof(float) * total, cudaMemcpyHostToDevice,
+                                                   s->stream));
+                    LGD_CHECK_CUDA(cudaStreamSynchronize(s->stream));
+                }
+            }
+            if (perm) {
+                LGD_CHECK_CUDA(cudaMalloc(&s->d_perm, sizeof(int) * n));
+                LGD_CHECK_CUDA(cudaMemcpyAsync(s->d_perm, perm, sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+            }
+            LGD_CHECK_CUDA(cudaStreamSynchronize(s->stream));
+        } catch (...) {
+            sell_free(*s);
+            delete s;
+            throw;
+        }
+        *out = reinterpret_cast<lgd_sell *>(s);
+    });
+}
+
+int lgd_sell_destroy(lgd_sell *h)
+{
+    return guard([&] {
+        if (!h) return;
+        Sell& s = sell_of(h);
+        sell_free(s);
+        delete &s;
+    });
+}
+
+static void sell_copy_x(Sell& s, int which, double *host, size_t bytes, bool up, bool logical)
+{
+    LGD_REQUIRE(which == 0 || which == 1, LGD_ERR_INVALID, "which must be 0 or 1");
+    LGD_REQUIRE(host != nullptr, LGD_ERR_INVALID, "null host buffer");
+    LGD_REQUIRE(bytes == sizeof(double) * (size_t)s.n, LGD_ERR_INVALID, "byte count must be n doubles");
+    LGD_REQUIRE(!logical || s.d_perm != nullptr, LGD_ERR_INVALID, "no permutation was given at create");
+    double *tmp = nullptr;
+    LGD_CHECK_CUDA(cudaMallocAsync(&tmp, bytes, s.stream));
+    void *x = s.d_x[which ? 1 - s.cur : s.cur];
+    const int *perm = logical ? s.d_perm : nullptr;
+    const int blocks = std::min(152 * 8, (s.n + 255) / 256);
+    if (up) {
+        LGD_CHECK_CUDA(cudaMemcpyAsync(tmp, host, bytes, cudaMemcpyHostToDevice, s.stream));
+        if (s.precision == 8) {
+            permute_in_kernel<double><<<blocks, 256, 0, s.stream>>>(tmp, perm, (double *)x, s.n);
+        } else {
+            permute_in_kernel<float><<<blocks, 256, 0, s.stream>>>(tmp, perm, (float *)x, s.n);
+        }
+    } else {
+        if (s.precision == 8) {
+            permute_out_kernel<double><<<blocks, 256, 0, s.stream>>>((const double *)x, perm, tmp, s.n);
+        } else {
+            permute_out_kernel<float><<<blocks, 256, 0, s.stream>>>((const float *)x, perm, tmp, s.n);
+        }
+        LGD_CHECK_CUDA(cudaMemcpyAsync(host, tmp, bytes, cudaMemcpyDeviceToHost, s.stream));
+    }
+    check_launch("sell permute");
+    ++s.launches;
+    LGD_CHECK_CUDA(cudaFreeAsync(tmp, s.stream));
+    LGD_CHECK_CUDA(cudaStreamSynchronize(s.stream));
+}
+
+int lgd_sell_upload_x(lgd_sell *h, int which, int logical, const double *x, size_t bytes)
+{
+    return guard([&] { sell_copy_x(sell_of(h), which, const_cast<double *>(x), bytes, true, logical != 0); });
+}
+
+int lgd_sell_download_x(lgd_sell *h, int which, int logical, double *x, size_t bytes)
+{
+    return guard([&] { sell_copy_x(sell_of(h), which, x, bytes, false, logical != 0); });
+}
+
+int lgd_sell_step(lgd_sell *h, int count)
+{
+    return guard([&] {
+        Sell& s = sell_of(h);
+        LGD_REQUIRE(count >= 0, LGD_ERR_INVALID, "negative step count");
+        for (int i = 0; i < count; ++i) {
+            launch_sell(s, 0, s.n);
+            s.cur = 1 - s.cur;
+        }
+    });
+}
+
+int lgd_sell_update_rows(lgd_sell *h, int row_begin, int row_end)
+{
+    return guard([&] {
+        Sell& s = sell_of(h);
+        LGD_REQUIRE(0 <= row_begin && row_begin <= row_end && row_end <= s.n, LGD_ERR_RANGE,
+                    "row range outside the node set");
+        launch_sell(s, row_begin, row_end);
+    });
+}
+
+int lgd_sell_swap(lgd_sell *h)
+{
+    return guard([&] {
+        Sell& s = sell_of(h);
+        s.cur = 1 - s.cur;
+    });
+}
+
+int lgd_sell_synchronize(lgd_sell *h)
+{
+    return guard([&] { LGD_CHECK_CUDA(cudaStreamSynchronize(sell_of(h).stream)); });
+}
+
+int lgd_sell_stream(lgd_sell *h, void **stream)
+{
+    return guard([&] {
+        LGD_REQUIRE(stream != nullptr, LGD_ERR_INVALID, "null output");
+        *stream = (void *)sell_of(h).stream;
+    });
+}
+
+int lgd_sell_launch_count(lgd_sell *h, uint64_t *count)
+{
+    return guard([&] {
+        LGD_REQUIRE(count != nullptr, LGD_ERR_INVALID, "null output");
+        *count = sell_of(h).launches;
+    });
+}
+
+}  // extern "C"

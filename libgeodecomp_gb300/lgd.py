@@ -89,6 +89,19 @@ def lib():
             "lgd_gpu_device_ptr": [P, I, I, P, P],
             "lgd_gpu_launch_count": [P, P],
             "lgd_gpu_set_time_block": [P, I],
+            "lgd_gpu_stream": [P, P],
+            "lgd_sell_plan": [I, P, I, I, P, P, P, P, P],
+            "lgd_sell_fill": [I, P, P, P, I, P, P, ctypes.c_int64, I, P, P],
+            "lgd_sell_create": [I, I, ctypes.c_int64, P, P, P, P, P, I, I, P],
+            "lgd_sell_destroy": [P],
+            "lgd_sell_upload_x": [P, I, I, P, S],
+            "lgd_sell_download_x": [P, I, I, P, S],
+            "lgd_sell_step": [P, I],
+            "lgd_sell_update_rows": [P, I, I],
+            "lgd_sell_swap": [P],
+            "lgd_sell_synchronize": [P],
+            "lgd_sell_stream": [P, P],
+            "lgd_sell_launch_count": [P, P],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -219,3 +232,97 @@ class Grid:
         e = ctypes.c_int()
         check(lib().lgd_gpu_fixed_point_exponent(self._h, ctypes.byref(e)))
         return e.value
+
+
+# ----------------------------------------------------------- SELL-C-sigma
+SELL_EXACT = 1
+
+
+def sell_build(n: int, row_ptr, col, w, C: int, sigma: int, remap_columns: bool = True) -> dict:
+    """SELL-C-sigma arrays from a logical CSR matrix (host-side builder of
+    the library; the layout is the reference's)."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    n_chunks = (n - 1) // C + 1
+    perm = np.zeros(n, dtype=np.int32)
+    row_length = np.zeros(n_chunks * C, dtype=np.int32)
+    chunk_length = np.zeros(n_chunks, dtype=np.int32)
+    chunk_offset = np.zeros(n_chunks + 1, dtype=np.int32)
+    total = ctypes.c_int64()
+    check(lib().lgd_sell_plan(n, _ptr(row_ptr), C, sigma, _ptr(perm), _ptr(row_length), _ptr(chunk_length),
+                              _ptr(chunk_offset), ctypes.byref(total)))
+    t = total.value
+    values = np.zeros(max(t, 1), dtype=np.float64)
+    column = np.zeros(max(t, 1), dtype=np.int32)
+    check(lib().lgd_sell_fill(n, _ptr(row_ptr), _ptr(col if col.size else np.zeros(1, np.int32)),
+                              _ptr(w if w.size else np.zeros(1)), C, _ptr(perm), _ptr(chunk_offset), t,
+                              int(remap_columns), _ptr(values), _ptr(column)))
+    return dict(perm=perm, row_length=row_length, chunk_length=chunk_length, chunk_offset=chunk_offset,
+                values=values[:t], column=column[:t], C=C, sigma=sigma, n=n)
+
+
+class SellGrid:
+    """Device SELL-C-sigma grid running the diffusion cell."""
+
+    def __init__(self, sell: dict, precision: int = 8, exact: bool = False):
+        self.n = sell["n"]
+        self._keep = [np.ascontiguousarray(sell[k]) for k in ("chunk_offset", "row_length", "values", "column", "perm")]
+        co, rl, vals, cols, perm = self._keep
+        if vals.size == 0:
+            vals = np.zeros(1)
+            cols = np.zeros(1, dtype=np.int32)
+        self._h = ctypes.c_void_p()
+        check(lib().lgd_sell_create(self.n, sell["C"], int(sell["values"].size), _ptr(co), _ptr(rl), _ptr(vals),
+                                    _ptr(cols), _ptr(perm), precision, SELL_EXACT if exact else 0,
+                                    ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            check(lib().lgd_sell_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, x: np.ndarray, logical: bool = True, which: int = 0):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        assert a.size == self.n
+        check(lib().lgd_sell_upload_x(self._h, which, int(logical), _ptr(a), a.nbytes))
+
+    def download(self, logical: bool = True, which: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.n, dtype=np.float64)
+        check(lib().lgd_sell_download_x(self._h, which, int(logical), _ptr(out), out.nbytes))
+        return out
+
+    def step(self, count: int = 1):
+        check(lib().lgd_sell_step(self._h, count))
+
+    def update_rows(self, begin: int, end: int):
+        check(lib().lgd_sell_update_rows(self._h, begin, end))
+
+    def swap(self):
+        check(lib().lgd_sell_swap(self._h))
+
+    def synchronize(self):
+        check(lib().lgd_sell_synchronize(self._h))
+
+    def stream(self) -> int:
+        p = ctypes.c_void_p()
+        check(lib().lgd_sell_stream(self._h, ctypes.byref(p)))
+        return p.value
+
+    def launch_count(self) -> int:
+        n = ctypes.c_uint64()
+        check(lib().lgd_sell_launch_count(self._h, ctypes.byref(n)))
+        return n.value

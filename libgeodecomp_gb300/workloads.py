@@ -154,7 +154,7 @@ def gaussian_random_field(n: int, length: float, seed: int, stream: int,
     ky = k[None, :, None]
     kx = np.fft.rfftfreq(n)[None, None, :] * 2.0 * np.pi
     filt = np.exp(-0.5 * (kx * kx + ky * ky + kz * kz) * length * length)
-    field = np.fft.irfftn(np.fft.rfftn(g) * filt, s=(n, n, n))
+    field = np.fft.irfftn(np.fft.rfftn(g) * filt, s=(n, n, n), axes=(0, 1, 2))
     fmin = field.min()
     fmax = field.max()
     return lo + (hi - lo) * (field - fmin) / (fmax - fmin)
