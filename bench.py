@@ -411,8 +411,8 @@ def cpu_stepper(name):
     import oracle
     from libgeodecomp_gb300 import workloads
     if name.startswith("jacobi7"):
-        u = workloads.jacobi_initial(512, 512, 512, seed=42)
-        return u.size, u, lambda a, s: oracle.jacobi7(a, s)
+        st = oracle.Jacobi7PingPong(workloads.jacobi_initial(512, 512, 512, seed=42))
+        return st.a.size, st, lambda a, s: a.step(s)
     if name == "gol_u8_8192":
         c = workloads.gol_initial(8192, 8192, seed=42)
         return c.size, c, lambda a, s: oracle.gol(a, s)

@@ -1,0 +1,71 @@
+/*
+ * lgd_ensemble.h - C ABI for batched ensembles of independent grids.
+ *
+ * An ensemble of D3Q19 BGK lid-driven cavities of uneven sizes advanced by
+ * one persistent kernel launch per time step, replayed from a CUDA graph.
+ * The reference has no ensemble runner; the per-instance semantics are
+ * those of one Simulator per grid (parallelization/serialsimulator.h:
+ * 76-139) running a D3Q19 cell (collision of
+ * src/examples/latticeboltzmann/main.cpp:93-170, pull scheme, bounce-back
+ * walls, moving lid beyond y = L-1).
+ *
+ * Instance layout (download/upload): 19 * L^3 doubles, population-major,
+ * f[i * L^3 + (z * L + y) * L + x], directions C, N, E, W, S, T, B, NW, SW,
+ * NE, SE, TW, BW, TE, BE, TN, BN, TS, BS (N = +y, E = +x, T = +z).
+ *
+ * Status codes and lgd_gpu_last_error() are shared with lgd_gpu.h.
+ */
+#ifndef LGD_ENSEMBLE_H
+#define LGD_ENSEMBLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "lgd_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lgd_lbm lgd_lbm;
+
+/* count instances with cube edges edges[j] in [2, 1024] and relaxation rates
+ * omegas[j] in (0, 2); lid velocity (lid, 0, 0); precision 4 (FP32) or 8
+ * (FP64).  All instances start in equilibrium at rest (f_i = w_i). */
+int lgd_lbm_create(int count, const int32_t *edges, const double *omegas, double lid, int precision, lgd_lbm **out);
+int lgd_lbm_destroy(lgd_lbm *h);
+
+/* steps time steps of every instance: one persistent launch per step. */
+int lgd_lbm_step(lgd_lbm *h, int steps);
+
+/* the same steps with one launch per instance and step (comparison path). */
+int lgd_lbm_step_looped(lgd_lbm *h, int steps);
+
+/* Launch shape: tile_rows rows of one z plane per work item, threads per
+ * CTA (64..1024, power of two), resident CTAs per SM (clamped to the
+ * occupancy limit). */
+int lgd_lbm_set_config(lgd_lbm *h, int tile_rows, int threads, int ctas_per_sm);
+int lgd_lbm_get_config(lgd_lbm *h, int *tile_rows, int *threads, int *ctas_per_sm);
+
+/* Pattern search over the launch shape, timing trial_steps steps per
+ * candidate with CUDA events; leaves the best shape set.  The trial steps
+ * advance the ensemble: reset or upload afterwards.  (Precedent: the
+ * reference's AutoTuningSimulator with PatternOptimizer,
+ * parallelization/autotuningsimulator.h:60-145, misc/patternoptimizer.h:13.) */
+int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int *ctas_per_sm, double *best_ms);
+
+/* Every instance back to equilibrium at rest. */
+int lgd_lbm_reset(lgd_lbm *h);
+
+int lgd_lbm_download(lgd_lbm *h, int instance, double *f, size_t bytes);
+int lgd_lbm_upload(lgd_lbm *h, int instance, const double *f, size_t bytes);
+int lgd_lbm_info(lgd_lbm *h, long long *total_cells, int *work_items);
+int lgd_lbm_synchronize(lgd_lbm *h);
+int lgd_lbm_stream(lgd_lbm *h, void **stream);
+int lgd_lbm_launch_count(lgd_lbm *h, uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

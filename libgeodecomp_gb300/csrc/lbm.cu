@@ -1,0 +1,633 @@
+// Batched ensemble of D3Q19 BGK lid-driven cavities.
+//
+// All instances live in one pair of allocations (A, B), each instance as
+// structure of arrays: population i of cell (x, y, z) of an L^3 instance at
+// base + i * L^3 + (z * L + y) * L + x.  Every time step is one persistent
+// kernel launch: the CTAs pull work items - TY rows of one z plane of one
+// instance, largest instances first - from an atomic counter until the list
+// is exhausted, so instances of 32^3 and 192^3 cells share the GPU without
+// per-instance launches.  Two steps (A -> B, B -> A, each with its counter
+// reset) are captured once into a CUDA graph and replayed.
+//
+// Cell update (pull scheme, the reference LBM example's incompressible BGK
+// collision, src/examples/latticeboltzmann/main.cpp:93-170): population i
+// comes from x - e_i; outside the box it is bounced back from the cell
+// itself, with 6 w_i (e_i . u_lid) added for populations coming from the
+// lid (the wall beyond y = L-1).  Traffic: 19 reads + 19 writes per cell and
+// step (152 B in FP32), the bounce-back reads hit L1.
+//
+// The tile height TY, threads per CTA and CTAs per SM are chosen by a
+// pattern search (lgd_lbm_tune), the method of the reference's
+// PatternOptimizer (misc/patternoptimizer.h:13) applied to this kernel.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "lgd_internal.h"
+#include "../../include/lgd_ensemble.h"
+
+namespace lgd {
+
+struct LbmInstance {
+    long long base;     // element offset of the instance in A and B
+    int L;
+    unsigned magic;     // ceil(2^32 / L), for row = c / L
+    float omega_f;
+    float lid_f;
+    double omega;
+    double lid;
+};
+
+struct Lbm {
+    int count;
+    int precision;
+    long long total_cells;
+    long long total_elems;
+    void *buf[2];
+    int cur;
+    LbmInstance *d_inst;
+    std::vector<LbmInstance> inst;
+    int4 *d_items;      // (instance, z, y0, y1)
+    int n_items;
+    int *d_counter;     // one per captured step
+    int ty, threads, ctas_per_sm;
+    int sms;
+    cudaStream_t stream;
+    cudaGraphExec_t graph;
+    bool graph_valid;
+    uint64_t launches;
+};
+
+// D3Q19 directions in the reference's naming order: C, N, E, W, S, T, B,
+// NW, SW, NE, SE, TW, BW, TE, BE, TN, BN, TS, BS (N = +y, E = +x, T = +z)
+__constant__ int c_ex[19] = {0, 0, 1, -1, 0, 0, 0, -1, -1, 1, 1, -1, -1, 1, 1, 0, 0, 0, 0};
+__constant__ int c_ey[19] = {0, 1, 0, 0, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1};
+__constant__ int c_ez[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+
+template<int I> struct Q;
+#define LGD_Q(I, EX, EY, EZ, OPP) \
+    template<> struct Q<I> { static const int ex = EX, ey = EY, ez = EZ, opp = OPP; };
+LGD_Q(0, 0, 0, 0, 0)
+LGD_Q(1, 0, 1, 0, 4)
+LGD_Q(2, 1, 0, 0, 3)
+LGD_Q(3, -1, 0, 0, 2)
+LGD_Q(4, 0, -1, 0, 1)
+LGD_Q(5, 0, 0, 1, 6)
+LGD_Q(6, 0, 0, -1, 5)
+LGD_Q(7, -1, 1, 0, 10)
+LGD_Q(8, -1, -1, 0, 9)
+LGD_Q(9, 1, 1, 0, 8)
+LGD_Q(10, 1, -1, 0, 7)
+LGD_Q(11, -1, 0, 1, 14)
+LGD_Q(12, -1, 0, -1, 13)
+LGD_Q(13, 1, 0, 1, 12)
+LGD_Q(14, 1, 0, -1, 11)
+LGD_Q(15, 0, 1, 1, 18)
+LGD_Q(16, 0, 1, -1, 17)
+LGD_Q(17, 0, -1, 1, 16)
+LGD_Q(18, 0, -1, -1, 15)
+#undef LGD_Q
+
+template<typename R>
+struct LbmArith;
+
+template<>
+struct LbmArith<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dadd_rn(a, -b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+};
+
+template<>
+struct LbmArith<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+};
+
+template<typename R, int I>
+__device__ __forceinline__ void pull_one(const R *__restrict__ src, long long n3, long long cell, int L, int x, int y,
+                                         int z, R lid, R *f)
+{
+    const int sx = x - Q<I>::ex;
+    const int sy = y - Q<I>::ey;
+    const int sz = z - Q<I>::ez;
+    if ((unsigned)sx < (unsigned)L && (unsigned)sy < (unsigned)L && (unsigned)sz < (unsigned)L) {
+        f[I] = src[I * n3 + cell - (Q<I>::ex + (long long)Q<I>::ey * L + (long long)Q<I>::ez * L * L)];
+    } else {
+        const R w = (I == 0) ? (R)(1.0 / 3.0) : ((I < 7) ? (R)(1.0 / 18.0) : (R)(1.0 / 36.0));
+        R v = src[Q<I>::opp * n3 + cell];
+        if (Q<I>::ey == -1 && Q<I>::ex != 0 && y == L - 1) {
+            // population from the lid: + 6 w_i (e_i . u_lid), u_lid = (lid, 0, 0);
+            // for every other wall the added term is exactly zero
+            v = LbmArith<R>::add(v, LbmArith<R>::mul(LbmArith<R>::mul((R)6.0, w), (R)Q<I>::ex * lid));
+        }
+        f[I] = v;
+    }
+}
+
+template<typename R, int I>
+struct PullAll {
+    static __device__ __forceinline__ void run(const R *src, long long n3, long long cell, int L, int x, int y, int z,
+                                               R lid, R *f)
+    {
+        pull_one<R, I>(src, n3, cell, L, x, y, z, lid, f);
+        PullAll<R, I + 1>::run(src, n3, cell, L, x, y, z, lid, f);
+    }
+};
+
+template<typename R>
+struct PullAll<R, 19> {
+    static __device__ __forceinline__ void run(const R *, long long, long long, int, int, int, int, R, R *) {}
+};
+
+// BGK collision, operation order of the oracle's lgd_d3q19_collide
+template<typename R>
+__device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict__ dst, long long n3, long long cell)
+{
+    typedef LbmArith<R> A;
+    R rho = f[0];
+#pragma unroll
+    for (int i = 1; i < 19; ++i) rho = A::add(rho, f[i]);
+    // E + NE + SE + TE + BE - (W + NW + SW + TW + BW)
+    const R ux = A::sub(A::add(A::add(A::add(A::add(f[2], f[9]), f[10]), f[13]), f[14]),
+                        A::add(A::add(A::add(A::add(f[3], f[7]), f[8]), f[11]), f[12]));
+    // N + NW + NE + TN + BN - (S + SW + SE + TS + BS)
+    const R uy = A::sub(A::add(A::add(A::add(A::add(f[1], f[7]), f[9]), f[15]), f[16]),
+                        A::add(A::add(A::add(A::add(f[4], f[8]), f[10]), f[17]), f[18]));
+    // T + TW + TE + TN + TS - (B + BW + BE + BN + BS)
+    const R uz = A::sub(A::add(A::add(A::add(A::add(f[5], f[11]), f[13]), f[15]), f[17]),
+                        A::add(A::add(A::add(A::add(f[6], f[12]), f[14]), f[16]), f[18]));
+    const R usq = A::add(A::add(A::mul(ux, ux), A::mul(uy, uy)), A::mul(uz, uz));
+    const R d = A::sub(A::mul(rho, (R)(1.0 / 3.0)), A::mul((R)0.5, usq));
+    const R keep = A::sub((R)1.0, omega);
+    const R w1 = A::mul(omega, (R)(1.0 / 6.0));
+    const R w2 = A::mul(omega, (R)(1.0 / 12.0));
+    dst[cell] = A::add(A::mul(keep, f[0]), A::mul(omega, d));
+#pragma unroll
+    for (int i = 1; i < 19; ++i) {
+        // eu = ex * ux + ey * uy + ez * uz, evaluated as the oracle does
+        const R eu = A::add(A::add(A::mul((R)c_ex[i], ux), A::mul((R)c_ey[i], uy)), A::mul((R)c_ez[i], uz));
+        const R wi = (i < 7) ? w1 : w2;
+        dst[i * n3 + cell] = A::add(A::mul(keep, f[i]), A::mul(wi, A::add(A::add(d, eu), A::mul((R)1.5, A::mul(eu, eu)))));
+    }
+}
+
+template<typename R>
+__device__ __forceinline__ void lbm_item(const LbmInstance& in, const R *__restrict__ A, R *__restrict__ B, int z, int y0,
+                                         int y1)
+{
+    const int L = in.L;
+    const long long n3 = (long long)L * L * L;
+    const R *src = A + in.base;
+    R *dst = B + in.base;
+    const R omega = (sizeof(R) == 8) ? (R)in.omega : (R)in.omega_f;
+    const R lid = (sizeof(R) == 8) ? (R)in.lid : (R)in.lid_f;
+    const unsigned cells = (unsigned)(y1 - y0) * (unsigned)L;
+    for (unsigned c = threadIdx.x; c < cells; c += blockDim.x) {
+        unsigned r = __umulhi(c, in.magic);
+        if (r * (unsigned)L > c) --r;
+        const int y = y0 + (int)r;
+        const int x = (int)(c - r * (unsigned)L);
+        const long long cell = ((long long)z * L + y) * L + x;
+        R f[19];
+        PullAll<R, 0>::run(src, n3, cell, L, x, y, z, lid, f);
+        collide_store<R>(f, omega, dst, n3, cell);
+    }
+}
+
+template<typename R>
+__global__ void lbm_persistent_kernel(const LbmInstance *__restrict__ inst, const int4 *__restrict__ items, int n_items,
+                                      int *counter, const R *__restrict__ A, R *__restrict__ B)
+{
+    __shared__ int s_item;
+    while (true) {
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const int4 w = items[it];
+        lbm_item<R>(inst[w.x], A, B, w.y, w.z, w.w);
+    }
+}
+
+// one instance, one launch: the looped single-grid comparison
+template<typename R>
+__global__ void lbm_single_kernel(const LbmInstance *__restrict__ inst, int j, const R *__restrict__ A, R *__restrict__ B)
+{
+    const LbmInstance in = inst[j];
+    const int z = blockIdx.y;
+    const int rows_per_block = max(1, (int)(blockDim.x / in.L));
+    const int y0 = blockIdx.x * rows_per_block;
+    if (y0 >= in.L) return;
+    lbm_item<R>(in, A, B, z, y0, min(in.L, y0 + rows_per_block));
+}
+
+template<typename R>
+__global__ void lbm_rest_kernel(const LbmInstance *__restrict__ inst, int count, R *A)
+{
+    const int j = blockIdx.y;
+    if (j >= count) return;
+    const LbmInstance in = inst[j];
+    const long long n3 = (long long)in.L * in.L * in.L;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n3; c += (long long)gridDim.x * blockDim.x) {
+        A[in.base + c] = (R)(1.0 / 3.0);
+        for (int i = 1; i < 7; ++i) A[in.base + i * n3 + c] = (R)(1.0 / 18.0);
+        for (int i = 7; i < 19; ++i) A[in.base + i * n3 + c] = (R)(1.0 / 36.0);
+    }
+}
+
+static Lbm& lbm_of(lgd_lbm *h)
+{
+    LGD_REQUIRE(h != nullptr, LGD_ERR_INVALID, "null handle");
+    return *reinterpret_cast<Lbm *>(h);
+}
+
+static void build_items(Lbm& e)
+{
+    // items of the largest instances first, so the tail of a step is made
+    // of small items
+    std::vector<int> order(e.count);
+    for (int j = 0; j < e.count; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e.inst[a].L > e.inst[b].L; });
+    std::vector<int4> items;
+    for (int j : order) {
+        const int L = e.inst[j].L;
+        for (int z = 0; z < L; ++z) {
+            for (int y0 = 0; y0 < L; y0 += e.ty) {
+                items.push_back(make_int4(j, z, y0, std::min(L, y0 + e.ty)));
+            }
+        }
+    }
+    if (e.d_items) cudaFree(e.d_items);
+    e.d_items = nullptr;
+    LGD_CHECK_CUDA(cudaMalloc(&e.d_items, sizeof(int4) * items.size()));
+    LGD_CHECK_CUDA(cudaMemcpyAsync(e.d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, e.stream));
+    LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+    e.n_items = (int)items.size();
+}
+
+static void launch_step(Lbm& e, int which_counter, int src)
+{
+    LGD_CHECK_CUDA(cudaMemsetAsync(e.d_counter + which_counter, 0, sizeof(int), e.stream));
+    const int grid = e.sms * e.ctas_per_sm;
+    if (e.precision == 4) {
+        lbm_persistent_kernel<float><<<grid, e.threads, 0, e.stream>>>(
+            e.d_inst, e.d_items, e.n_items, e.d_counter + which_counter, (const float *)e.buf[src], (float *)e.buf[1 - src]);
+    } else {
+        lbm_persistent_kernel<double><<<grid, e.threads, 0, e.stream>>>(
+            e.d_inst, e.d_items, e.n_items, e.d_counter + which_counter, (const double *)e.buf[src], (double *)e.buf[1 - src]);
+    }
+    check_launch("lbm persistent");
+}
+
+static void rebuild_graph(Lbm& e)
+{
+    if (e.graph_valid) {
+        cudaGraphExecDestroy(e.graph);
+        e.graph_valid = false;
+    }
+    cudaGraph_t g;
+    LGD_CHECK_CUDA(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        launch_step(e, 0, 0);
+        launch_step(e, 1, 1);
+    } catch (...) {
+        cudaStreamEndCapture(e.stream, &g);
+        throw;
+    }
+    LGD_CHECK_CUDA(cudaStreamEndCapture(e.stream, &g));
+    cudaError_t err = cudaGraphInstantiate(&e.graph, g, 0);
+    cudaGraphDestroy(g);
+    LGD_CHECK_CUDA(err);
+    e.graph_valid = true;
+}
+
+static void set_config(Lbm& e, int ty, int threads, int ctas)
+{
+    LGD_REQUIRE(ty >= 1 && ty <= 1024, LGD_ERR_INVALID, "tile rows out of range");
+    LGD_REQUIRE(threads == 64 || threads == 128 || threads == 256 || threads == 512 || threads == 1024, LGD_ERR_INVALID,
+                "threads per CTA must be a power of two in [64, 1024]");
+    LGD_REQUIRE(ctas >= 1 && ctas <= 32, LGD_ERR_INVALID, "CTAs per SM out of range");
+    int max_ctas = 0;
+    if (e.precision == 4) {
+        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_ctas, lbm_persistent_kernel<float>, threads, 0));
+    } else {
+        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_ctas, lbm_persistent_kernel<double>, threads, 0));
+    }
+    LGD_REQUIRE(max_ctas >= 1, LGD_ERR_INVALID, "kernel does not fit with this many threads");
+    ctas = std::min(ctas, max_ctas);   // a persistent grid never exceeds what is resident
+    const bool items_change = (ty != e.ty) || e.d_items == nullptr;
+    e.ty = ty;
+    e.threads = threads;
+    e.ctas_per_sm = ctas;
+    if (items_change) build_items(e);
+    rebuild_graph(e);
+}
+
+static void run_steps(Lbm& e, int steps)
+{
+    int s = 0;
+    if (e.cur == 1 && steps > 0) {
+        launch_step(e, 0, 1);
+        ++e.launches;
+        e.cur = 0;
+        ++s;
+    }
+    for (; s + 1 < steps; s += 2) {
+        LGD_CHECK_CUDA(cudaGraphLaunch(e.graph, e.stream));
+        e.launches += 2;
+    }
+    if (s < steps) {
+        launch_step(e, 0, 0);
+        ++e.launches;
+        e.cur = 1;
+    }
+}
+
+static void lbm_free(Lbm& e)
+{
+    if (e.stream) cudaStreamSynchronize(e.stream);
+    if (e.graph_valid) cudaGraphExecDestroy(e.graph);
+    cudaFree(e.buf[0]);
+    cudaFree(e.buf[1]);
+    cudaFree(e.d_inst);
+    cudaFree(e.d_items);
+    cudaFree(e.d_counter);
+    if (e.stream) cudaStreamDestroy(e.stream);
+}
+
+}  // namespace lgd
+
+using namespace lgd;
+
+extern "C" {
+
+int lgd_lbm_create(int count, const int32_t *edges, const double *omegas, double lid, int precision, lgd_lbm **out)
+{
+    return guard([&] {
+        LGD_REQUIRE(out != nullptr, LGD_ERR_INVALID, "null output");
+        *out = nullptr;
+        LGD_REQUIRE(count > 0 && edges && omegas, LGD_ERR_INVALID, "need at least one instance");
+        LGD_REQUIRE(precision == 4 || precision == 8, LGD_ERR_INVALID, "precision must be 4 (FP32) or 8 (FP64)");
+        Lbm *e = new Lbm();
+        e->count = count;
+        e->precision = precision;
+        e->inst.resize(count);
+        long long off = 0;
+        for (int j = 0; j < count; ++j) {
+            LGD_REQUIRE(edges[j] >= 2 && edges[j] <= 1024, LGD_ERR_RANGE, "instance edge must lie in [2, 1024]");
+            LGD_REQUIRE(omegas[j] > 0.0 && omegas[j] < 2.0, LGD_ERR_RANGE, "omega must lie in (0, 2)");
+            LbmInstance& in = e->inst[j];
+            in.base = off;
+            in.L = edges[j];
+            in.magic = (unsigned)((0x100000000ull + edges[j] - 1) / edges[j]);
+            in.omega = omegas[j];
+            in.lid = lid;
+            in.omega_f = (float)omegas[j];
+            in.lid_f = (float)lid;
+            const long long n3 = (long long)edges[j] * edges[j] * edges[j];
+            off += 19 * n3;
+            e->total_cells += n3;
+            LGD_REQUIRE(n3 * 19 < (1ll << 31) * 16, LGD_ERR_RANGE, "instance too large");
+        }
+        e->total_elems = off;
+        int dev = 0;
+        try {
+            LGD_CHECK_CUDA(cudaGetDevice(&dev));
+            LGD_CHECK_CUDA(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev));
+            LGD_CHECK_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+            for (int b = 0; b < 2; ++b) LGD_CHECK_CUDA(cudaMalloc(&e->buf[b], (size_t)precision * off));
+            LGD_CHECK_CUDA(cudaMalloc(&e->d_inst, sizeof(LbmInstance) * count));
+            LGD_CHECK_CUDA(cudaMemcpyAsync(e->d_inst, e->inst.data(), sizeof(LbmInstance) * count,
+                                           cudaMemcpyHostToDevice, e->stream));
+            LGD_CHECK_CUDA(cudaMalloc(&e->d_counter, sizeof(int) * 2));
+            dim3 grid(256, count);
+            if (precision == 4) {
+                lbm_rest_kernel<float><<<grid, 256, 0, e->stream>>>(e->d_inst, count, (float *)e->buf[0]);
+            } else {
+                lbm_rest_kernel<double><<<grid, 256, 0, e->stream>>>(e->d_inst, count, (double *)e->buf[0]);
+            }
+            check_launch("lbm rest state");
+            ++e->launches;
+            set_config(*e, 4, 256, 4);
+        } catch (...) {
+            lbm_free(*e);
+            delete e;
+            throw;
+        }
+        *out = reinterpret_cast<lgd_lbm *>(e);
+    });
+}
+
+int lgd_lbm_destroy(lgd_lbm *h)
+{
+    return guard([&] {
+        if (!h) return;
+        Lbm& e = lbm_of(h);
+        lbm_free(e);
+        delete &e;
+    });
+}
+
+int lgd_lbm_step(lgd_lbm *h, int steps)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        LGD_REQUIRE(steps >= 0, LGD_ERR_INVALID, "negative step count");
+        run_steps(e, steps);
+    });
+}
+
+int lgd_lbm_step_looped(lgd_lbm *h, int steps)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        LGD_REQUIRE(steps >= 0, LGD_ERR_INVALID, "negative step count");
+        for (int s = 0; s < steps; ++s) {
+            for (int j = 0; j < e.count; ++j) {
+                const int L = e.inst[j].L;
+                const int rows = std::max(1, 256 / L);
+                dim3 grid((L + rows - 1) / rows, L);
+                if (e.precision == 4) {
+                    lbm_single_kernel<float><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const float *)e.buf[e.cur],
+                                                                         (float *)e.buf[1 - e.cur]);
+                } else {
+                    lbm_single_kernel<double><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const double *)e.buf[e.cur],
+                                                                          (double *)e.buf[1 - e.cur]);
+                }
+                check_launch("lbm single");
+                ++e.launches;
+            }
+            e.cur = 1 - e.cur;
+        }
+    });
+}
+
+int lgd_lbm_set_config(lgd_lbm *h, int tile_rows, int threads, int ctas_per_sm)
+{
+    return guard([&] { set_config(lbm_of(h), tile_rows, threads, ctas_per_sm); });
+}
+
+int lgd_lbm_get_config(lgd_lbm *h, int *tile_rows, int *threads, int *ctas_per_sm)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        if (tile_rows) *tile_rows = e.ty;
+        if (threads) *threads = e.threads;
+        if (ctas_per_sm) *ctas_per_sm = e.ctas_per_sm;
+    });
+}
+
+int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int *ctas_per_sm, double *best_ms)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        LGD_REQUIRE(trial_steps >= 2, LGD_ERR_INVALID, "trial_steps must be at least 2");
+        cudaEvent_t t0, t1;
+        LGD_CHECK_CUDA(cudaEventCreate(&t0));
+        LGD_CHECK_CUDA(cudaEventCreate(&t1));
+        // the trial runs advance the ensemble: callers reset or upload afterwards
+        auto measure = [&](int ty, int th, int ct) -> double {
+            set_config(e, ty, th, ct);
+            run_steps(e, 2);   // warm
+            LGD_CHECK_CUDA(cudaEventRecord(t0, e.stream));
+            run_steps(e, trial_steps);
+            LGD_CHECK_CUDA(cudaEventRecord(t1, e.stream));
+            LGD_CHECK_CUDA(cudaEventSynchronize(t1));
+            float ms = 0.f;
+            LGD_CHECK_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+            return ms / trial_steps;
+        };
+        // pattern search over (log2 tile rows, log2 threads, CTAs per SM)
+        const int tys[] = {1, 2, 4, 8, 16, 32};
+        const int ths[] = {128, 256, 512};
+        const int cts[] = {1, 2, 3, 4, 6, 8};
+        int a = 2, b = 1, c = 3;   // start at (4, 256, 4)
+        double best = measure(tys[a], ths[b], cts[c]);
+        bool moved = true;
+        int evals = 1;
+        while (moved && evals < 40) {
+            moved = false;
+            const int da[6] = {-1, 1, 0, 0, 0, 0};
+            const int db[6] = {0, 0, -1, 1, 0, 0};
+            const int dc[6] = {0, 0, 0, 0, -1, 1};
+            int ba = a, bb = b, bc = c;
+            for (int k = 0; k < 6; ++k) {
+                const int na = a + da[k], nb = b + db[k], nc = c + dc[k];
+                if (na < 0 || na >= 6 || nb < 0 || nb >= 3 || nc < 0 || nc >= 6) continue;
+                const double t = measure(tys[na], ths[nb], cts[nc]);
+                ++evals;
+                if (t < best * 0.99) {
+                    best = t;
+                    ba = na;
+                    bb = nb;
+                    bc = nc;
+                    moved = true;
+                }
+            }
+            a = ba;
+            b = bb;
+            c = bc;
+        }
+        set_config(e, tys[a], ths[b], cts[c]);
+        LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        if (tile_rows) *tile_rows = e.ty;
+        if (threads) *threads = e.threads;
+        if (ctas_per_sm) *ctas_per_sm = e.ctas_per_sm;
+        if (best_ms) *best_ms = best;
+    });
+}
+
+int lgd_lbm_reset(lgd_lbm *h)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        dim3 grid(256, e.count);
+        if (e.precision == 4) {
+            lbm_rest_kernel<float><<<grid, 256, 0, e.stream>>>(e.d_inst, e.count, (float *)e.buf[0]);
+        } else {
+            lbm_rest_kernel<double><<<grid, 256, 0, e.stream>>>(e.d_inst, e.count, (double *)e.buf[0]);
+        }
+        check_launch("lbm rest state");
+        ++e.launches;
+        e.cur = 0;
+        LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+    });
+}
+
+int lgd_lbm_download(lgd_lbm *h, int instance, double *f, size_t bytes)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        LGD_REQUIRE(instance >= 0 && instance < e.count, LGD_ERR_RANGE, "instance out of range");
+        const LbmInstance& in = e.inst[instance];
+        const size_t n = 19ull * in.L * in.L * in.L;
+        LGD_REQUIRE(f != nullptr && bytes == n * sizeof(double), LGD_ERR_INVALID, "buffer must hold 19 * L^3 doubles");
+        if (e.precision == 8) {
+            LGD_CHECK_CUDA(cudaMemcpyAsync(f, (const double *)e.buf[e.cur] + in.base, bytes, cudaMemcpyDeviceToHost, e.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+        } else {
+            std::vector<float> tmp(n);
+            LGD_CHECK_CUDA(cudaMemcpyAsync(tmp.data(), (const float *)e.buf[e.cur] + in.base, n * 4, cudaMemcpyDeviceToHost,
+                                           e.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+            for (size_t i = 0; i < n; ++i) f[i] = tmp[i];
+        }
+    });
+}
+
+int lgd_lbm_upload(lgd_lbm *h, int instance, const double *f, size_t bytes)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        LGD_REQUIRE(instance >= 0 && instance < e.count, LGD_ERR_RANGE, "instance out of range");
+        const LbmInstance& in = e.inst[instance];
+        const size_t n = 19ull * in.L * in.L * in.L;
+        LGD_REQUIRE(f != nullptr && bytes == n * sizeof(double), LGD_ERR_INVALID, "buffer must hold 19 * L^3 doubles");
+        if (e.precision == 8) {
+            LGD_CHECK_CUDA(cudaMemcpyAsync((double *)e.buf[e.cur] + in.base, f, bytes, cudaMemcpyHostToDevice, e.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+        } else {
+            std::vector<float> tmp(f, f + n);
+            LGD_CHECK_CUDA(cudaMemcpyAsync((float *)e.buf[e.cur] + in.base, tmp.data(), n * 4, cudaMemcpyHostToDevice,
+                                           e.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+        }
+    });
+}
+
+int lgd_lbm_info(lgd_lbm *h, long long *total_cells, int *work_items)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        if (total_cells) *total_cells = e.total_cells;
+        if (work_items) *work_items = e.n_items;
+    });
+}
+
+int lgd_lbm_synchronize(lgd_lbm *h)
+{
+    return guard([&] { LGD_CHECK_CUDA(cudaStreamSynchronize(lbm_of(h).stream)); });
+}
+
+int lgd_lbm_stream(lgd_lbm *h, void **stream)
+{
+    return guard([&] {
+        LGD_REQUIRE(stream != nullptr, LGD_ERR_INVALID, "null output");
+        *stream = (void *)lbm_of(h).stream;
+    });
+}
+
+int lgd_lbm_launch_count(lgd_lbm *h, uint64_t *count)
+{
+    return guard([&] {
+        LGD_REQUIRE(count != nullptr, LGD_ERR_INVALID, "null output");
+        *count = lbm_of(h).launches;
+    });
+}
+
+}  // extern "C"

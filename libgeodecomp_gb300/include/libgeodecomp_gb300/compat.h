@@ -1,0 +1,523 @@
+// Host-side mirror of the part of LibGeoDecomp's public API that
+// GB300Simulator and its plugins touch, for builds without the reference's
+// headers (the reference library is header-only C++ and may not be
+// installed where the GPU library runs).  Names, signatures and event
+// semantics follow the reference so that plugin code compiles unchanged
+// against either:
+//   Coord / CoordBox / Streak / Region      geometry/coord.h, coordbox.h,
+//                                           streak.h, region.h
+//   Topologies::Cube / Torus, WrapsAxis     geometry/topologies.h:179-278
+//   Stencils::Moore / VonNeumann            geometry/stencils.h:182-227
+//   APITraits (topology, nano steps, tags)  misc/apitraits.h:69-836
+//   GridBase, DisplacedGrid                 storage/gridbase.h:71,
+//                                           storage/displacedgrid.h:116
+//   Initializer, SimpleInitializer          io/initializer.h:22-71,
+//                                           io/simpleinitializer.h
+//   Writer, WriterEvent                     io/writer.h:14-90
+//   Steerer, SteererEvent, SteererFeedback  io/steerer.h:11-140
+//   Simulator, MonolithicSimulator          parallelization/simulator.h:28-106,
+//                                           parallelization/monolithicsimulator.h:16-52
+// Only what a single-node simulator needs is here: no MPI, no HPX, no
+// serialisation, no region algebra beyond streak lists.
+#ifndef LGD_GB300_COMPAT_H
+#define LGD_GB300_COMPAT_H
+
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace LibGeoDecomp {
+
+template<typename T>
+struct SharedPtr {
+    typedef std::shared_ptr<T> Type;
+};
+
+// ------------------------------------------------------------------ Coord
+template<int DIM>
+class Coord;
+
+template<>
+class Coord<1> {
+public:
+    explicit Coord(int x = 0) { c[0] = x; }
+    int x() const { return c[0]; }
+    int& operator[](int i) { return c[i]; }
+    int operator[](int i) const { return c[i]; }
+    long prod() const { return c[0]; }
+    bool operator==(const Coord& o) const { return c[0] == o.c[0]; }
+    bool operator!=(const Coord& o) const { return !(*this == o); }
+    Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0]); }
+    Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0]); }
+    static Coord diagonal(int v) { return Coord(v); }
+
+private:
+    int c[1];
+};
+
+template<>
+class Coord<2> {
+public:
+    explicit Coord(int x = 0, int y = 0) { c[0] = x; c[1] = y; }
+    int x() const { return c[0]; }
+    int y() const { return c[1]; }
+    int& operator[](int i) { return c[i]; }
+    int operator[](int i) const { return c[i]; }
+    long prod() const { return (long)c[0] * c[1]; }
+    bool operator==(const Coord& o) const { return c[0] == o.c[0] && c[1] == o.c[1]; }
+    bool operator!=(const Coord& o) const { return !(*this == o); }
+    Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0], c[1] + o.c[1]); }
+    Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0], c[1] - o.c[1]); }
+    static Coord diagonal(int v) { return Coord(v, v); }
+
+private:
+    int c[2];
+};
+
+template<>
+class Coord<3> {
+public:
+    explicit Coord(int x = 0, int y = 0, int z = 0) { c[0] = x; c[1] = y; c[2] = z; }
+    int x() const { return c[0]; }
+    int y() const { return c[1]; }
+    int z() const { return c[2]; }
+    int& operator[](int i) { return c[i]; }
+    int operator[](int i) const { return c[i]; }
+    long prod() const { return (long)c[0] * c[1] * c[2]; }
+    bool operator==(const Coord& o) const { return c[0] == o.c[0] && c[1] == o.c[1] && c[2] == o.c[2]; }
+    bool operator!=(const Coord& o) const { return !(*this == o); }
+    Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0], c[1] + o.c[1], c[2] + o.c[2]); }
+    Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0], c[1] - o.c[1], c[2] - o.c[2]); }
+    static Coord diagonal(int v) { return Coord(v, v, v); }
+
+private:
+    int c[3];
+};
+
+// --------------------------------------------------------------- CoordBox
+template<int DIM>
+class CoordBox {
+public:
+    class Iterator {
+    public:
+        Iterator(const Coord<DIM>& origin, const Coord<DIM>& dim, const Coord<DIM>& cursor) :
+            origin(origin), dim(dim), cursor(cursor)
+        {}
+        const Coord<DIM>& operator*() const { return cursor; }
+        const Coord<DIM> *operator->() const { return &cursor; }
+        bool operator!=(const Iterator& o) const { return cursor != o.cursor; }
+        bool operator==(const Iterator& o) const { return cursor == o.cursor; }
+        Iterator& operator++()
+        {
+            for (int d = 0; d < DIM; ++d) {
+                ++cursor[d];
+                if (cursor[d] < origin[d] + dim[d] || d == DIM - 1) {
+                    return *this;
+                }
+                cursor[d] = origin[d];
+            }
+            return *this;
+        }
+
+    private:
+        Coord<DIM> origin;
+        Coord<DIM> dim;
+        Coord<DIM> cursor;
+    };
+
+    explicit CoordBox(const Coord<DIM>& origin = Coord<DIM>(), const Coord<DIM>& dimensions = Coord<DIM>()) :
+        origin(origin), dimensions(dimensions)
+    {}
+
+    bool inBounds(const Coord<DIM>& c) const
+    {
+        for (int d = 0; d < DIM; ++d) {
+            if (c[d] < origin[d] || c[d] >= origin[d] + dimensions[d]) return false;
+        }
+        return true;
+    }
+
+    std::size_t size() const { return (std::size_t)dimensions.prod(); }
+
+    Iterator begin() const { return Iterator(origin, dimensions, origin); }
+
+    Iterator end() const
+    {
+        if (dimensions.prod() == 0) return begin();
+        Coord<DIM> c = origin;
+        c[DIM - 1] = origin[DIM - 1] + dimensions[DIM - 1];
+        return Iterator(origin, dimensions, c);
+    }
+
+    Coord<DIM> origin;
+    Coord<DIM> dimensions;
+};
+
+// ---------------------------------------------------------- Streak, Region
+template<int DIM>
+class Streak {
+public:
+    Streak(const Coord<DIM>& origin = Coord<DIM>(), int endX = 0) : origin(origin), endX(endX) {}
+    int length() const { return endX - origin.x(); }
+    Coord<DIM> origin;
+    int endX;
+};
+
+// A region as an ordered list of streaks (no overlap handling).
+template<int DIM>
+class Region {
+public:
+    typedef typename std::vector<Streak<DIM> >::const_iterator StreakIterator;
+
+    Region& operator<<(const Streak<DIM>& s)
+    {
+        if (s.endX > s.origin.x()) streaks.push_back(s);
+        return *this;
+    }
+
+    Region& operator<<(const CoordBox<DIM>& box)
+    {
+        if (box.size() == 0) return *this;
+        Coord<DIM> row = box.origin;
+        CoordBox<DIM> rows = box;
+        rows.dimensions[0] = 1;
+        for (typename CoordBox<DIM>::Iterator i = rows.begin(); i != rows.end(); ++i) {
+            *this << Streak<DIM>(*i, i->x() + box.dimensions.x());
+        }
+        (void)row;
+        return *this;
+    }
+
+    StreakIterator beginStreak() const { return streaks.begin(); }
+    StreakIterator endStreak() const { return streaks.end(); }
+    std::size_t numStreaks() const { return streaks.size(); }
+
+    std::size_t size() const
+    {
+        std::size_t n = 0;
+        for (StreakIterator i = beginStreak(); i != endStreak(); ++i) n += i->length();
+        return n;
+    }
+
+private:
+    std::vector<Streak<DIM> > streaks;
+};
+
+// ------------------------------------------------------------- topologies
+namespace Topologies {
+
+template<int DIMENSIONS, bool WRAP>
+class TopologyTemplate {
+public:
+    static const int DIM = DIMENSIONS;
+    template<int D>
+    class WrapsAxis {
+    public:
+        static const bool VALUE = WRAP && (D < DIMENSIONS);
+    };
+
+    static Coord<DIM> normalize(Coord<DIM> c, const Coord<DIM>& dim)
+    {
+        for (int d = 0; d < DIM; ++d) {
+            if (WRAP) c[d] = ((c[d] % dim[d]) + dim[d]) % dim[d];
+        }
+        return c;
+    }
+};
+
+template<int DIM>
+class Cube {
+public:
+    typedef TopologyTemplate<DIM, false> Topology;
+};
+
+template<int DIM>
+class Torus {
+public:
+    typedef TopologyTemplate<DIM, true> Topology;
+};
+
+}  // namespace Topologies
+
+namespace Stencils {
+template<int DIM, int RADIUS>
+class VonNeumann {
+public:
+    static const int DIMENSIONS = DIM;
+};
+template<int DIM, int RADIUS>
+class Moore {
+public:
+    static const int DIMENSIONS = DIM;
+};
+}  // namespace Stencils
+
+// -------------------------------------------------------------- APITraits
+class APITraits {
+public:
+    template<typename CELL, typename HAS = void>
+    class SelectTopology {
+    public:
+        typedef Topologies::Cube<2>::Topology Value;
+    };
+
+    template<typename CELL>
+    class SelectTopology<CELL, typename CELL::API::SupportsTopology> {
+    public:
+        typedef typename CELL::API::Topology Value;
+    };
+
+    template<typename CELL, typename HAS = void>
+    class SelectNanoSteps {
+    public:
+        static const unsigned VALUE = 1;
+    };
+
+    template<typename CELL>
+    class SelectNanoSteps<CELL, typename CELL::API::SupportsNanoSteps> {
+    public:
+        static const unsigned VALUE = CELL::API::NANO_STEPS;
+    };
+
+    template<typename TOPOLOGY>
+    class HasTopology {
+    public:
+        typedef void SupportsTopology;
+        typedef TOPOLOGY Topology;
+    };
+
+    template<int DIM>
+    class HasCubeTopology : public HasTopology<typename Topologies::Cube<DIM>::Topology> {};
+
+    template<int DIM>
+    class HasTorusTopology : public HasTopology<typename Topologies::Torus<DIM>::Topology> {};
+
+    template<unsigned N>
+    class HasNanoSteps {
+    public:
+        typedef void SupportsNanoSteps;
+        static const unsigned NANO_STEPS = N;
+    };
+
+    template<typename STENCIL>
+    class HasStencil {
+    public:
+        typedef STENCIL Stencil;
+    };
+
+    class HasSoA {};
+    class HasUpdateLineX {};
+    class HasFixedCoordsOnlyUpdate {};
+};
+
+// ------------------------------------------------------------------ grids
+template<typename CELL, int DIMENSIONS>
+class GridBase {
+public:
+    static const int DIM = DIMENSIONS;
+    typedef CELL CellType;
+
+    virtual ~GridBase() {}
+    virtual void set(const Coord<DIM>& c, const CELL& cell) = 0;
+    virtual CELL get(const Coord<DIM>& c) const = 0;
+    virtual void setEdge(const CELL& cell) = 0;
+    virtual const CELL& getEdge() const = 0;
+    virtual CoordBox<DIM> boundingBox() const = 0;
+    Coord<DIM> dimensions() const { return boundingBox().dimensions; }
+};
+
+// Host grid with the cells in x-fastest order plus one edge cell.
+template<typename CELL, typename TOPOLOGY = Topologies::Cube<2>::Topology, bool TOPOLOGICALLY_CORRECT = false>
+class DisplacedGrid : public GridBase<CELL, TOPOLOGY::DIM> {
+public:
+    static const int DIM = TOPOLOGY::DIM;
+
+    explicit DisplacedGrid(const CoordBox<DIM>& box = CoordBox<DIM>(), const CELL& defaultCell = CELL(),
+                           const CELL& edgeCell = CELL()) :
+        box(box), cells(box.size(), defaultCell), edge(edgeCell)
+    {}
+
+    void set(const Coord<DIM>& c, const CELL& cell) { cells[index(c)] = cell; }
+    CELL get(const Coord<DIM>& c) const { return cells[index(c)]; }
+    CELL& operator[](const Coord<DIM>& c) { return cells[index(c)]; }
+    const CELL& operator[](const Coord<DIM>& c) const { return cells[index(c)]; }
+    void setEdge(const CELL& cell) { edge = cell; }
+    const CELL& getEdge() const { return edge; }
+    CoordBox<DIM> boundingBox() const { return box; }
+    CELL *data() { return cells.data(); }
+    const CELL *data() const { return cells.data(); }
+
+private:
+    CoordBox<DIM> box;
+    std::vector<CELL> cells;
+    CELL edge;
+
+    std::size_t index(const Coord<DIM>& c) const
+    {
+        std::size_t i = 0;
+        for (int d = DIM - 1; d >= 0; --d) {
+            const int v = c[d] - box.origin[d];
+            if (v < 0 || v >= box.dimensions[d]) throw std::out_of_range("coordinate outside the grid");
+            i = i * box.dimensions[d] + v;
+        }
+        return i;
+    }
+};
+
+// ------------------------------------------------------------ Initializer
+template<typename CELL>
+class Initializer {
+public:
+    typedef typename APITraits::SelectTopology<CELL>::Value Topology;
+    typedef CELL Cell;
+    static const unsigned NANO_STEPS = APITraits::SelectNanoSteps<CELL>::VALUE;
+    static const int DIM = Topology::DIM;
+
+    virtual ~Initializer() {}
+    virtual void grid(GridBase<CELL, DIM> *target) = 0;
+    virtual CoordBox<DIM> gridBox() { return CoordBox<DIM>(Coord<DIM>(), gridDimensions()); }
+    virtual Coord<DIM> gridDimensions() const = 0;
+    virtual unsigned startStep() const = 0;
+    virtual unsigned maxSteps() const = 0;
+};
+
+template<typename CELL>
+class SimpleInitializer : public Initializer<CELL> {
+public:
+    typedef typename Initializer<CELL>::Topology Topology;
+    static const int DIM = Topology::DIM;
+
+    explicit SimpleInitializer(const Coord<DIM>& dimensions, const unsigned steps = 300) :
+        dimensions(dimensions), steps(steps)
+    {}
+
+    Coord<DIM> gridDimensions() const { return dimensions; }
+    unsigned maxSteps() const { return steps; }
+    unsigned startStep() const { return 0; }
+
+protected:
+    Coord<DIM> dimensions;
+    unsigned steps;
+};
+
+// ----------------------------------------------------------------- Writer
+enum WriterEvent {
+    WRITER_INITIALIZED,
+    WRITER_STEP_FINISHED,
+    WRITER_ALL_DONE
+};
+
+template<typename CELL>
+class Writer {
+public:
+    typedef typename APITraits::SelectTopology<CELL>::Value Topology;
+    static const int DIM = Topology::DIM;
+    typedef GridBase<CELL, DIM> GridType;
+
+    Writer(const std::string& prefix, const unsigned period) : prefix(prefix), period(period)
+    {
+        if (period == 0) throw std::invalid_argument("period must be positive");
+    }
+
+    virtual ~Writer() {}
+    virtual Writer *clone() const = 0;
+    virtual void stepFinished(const GridType& grid, unsigned step, WriterEvent event) = 0;
+    unsigned getPeriod() const { return period; }
+    const std::string& getPrefix() const { return prefix; }
+
+protected:
+    std::string prefix;
+    unsigned period;
+};
+
+// ---------------------------------------------------------------- Steerer
+enum SteererEvent {
+    STEERER_INITIALIZED,
+    STEERER_NEXT_STEP,
+    STEERER_ALL_DONE
+};
+
+template<typename CELL>
+class Steerer {
+public:
+    typedef typename APITraits::SelectTopology<CELL>::Value Topology;
+    typedef GridBase<CELL, Topology::DIM> GridType;
+    typedef Coord<Topology::DIM> CoordType;
+
+    class SteererFeedback {
+    public:
+        SteererFeedback() : simulationEnd(false) {}
+        void endSimulation() { simulationEnd = true; }
+        bool simulationEnded() { return simulationEnd; }
+
+    private:
+        bool simulationEnd;
+    };
+
+    explicit Steerer(const unsigned period) : period(period) {}
+    virtual ~Steerer() {}
+    virtual void setRegion(const Region<Topology::DIM>& newRegion) { region = newRegion; }
+    virtual void nextStep(GridType *grid, const Region<Topology::DIM>& validRegion, const CoordType& globalDimensions,
+                          unsigned step, SteererEvent event, std::size_t rank, bool lastCall,
+                          SteererFeedback *feedback) = 0;
+    unsigned getPeriod() const { return period; }
+
+protected:
+    Region<Topology::DIM> region;
+    unsigned period;
+};
+
+// -------------------------------------------------------------- Simulator
+class Chronometer {};
+
+template<typename CELL>
+class Simulator {
+public:
+    typedef typename APITraits::SelectTopology<CELL>::Value Topology;
+    static const int DIM = Topology::DIM;
+    static const unsigned NANO_STEPS = APITraits::SelectNanoSteps<CELL>::VALUE;
+    typedef GridBase<CELL, DIM> GridType;
+    typedef typename SharedPtr<Initializer<CELL> >::Type InitPtr;
+    typedef typename SharedPtr<Steerer<CELL> >::Type SteererPtr;
+    typedef std::vector<SteererPtr> SteererVector;
+
+    explicit Simulator(Initializer<CELL> *initializer) :
+        stepNum(0), initializer(initializer), gridDim(initializer->gridDimensions())
+    {}
+
+    virtual ~Simulator() {}
+    virtual void step() = 0;
+    virtual void run() = 0;
+    virtual unsigned getStep() const { return stepNum; }
+    virtual InitPtr getInitializer() const { return initializer; }
+    virtual void addSteerer(Steerer<CELL> *steerer) { steerers.push_back(SteererPtr(steerer)); }
+    virtual std::vector<Chronometer> gatherStatistics() = 0;
+
+protected:
+    Chronometer chronometer;
+    unsigned stepNum;
+    InitPtr initializer;
+    SteererVector steerers;
+    Coord<DIM> gridDim;
+};
+
+template<typename CELL>
+class MonolithicSimulator : public Simulator<CELL> {
+public:
+    typedef typename SharedPtr<Writer<CELL> >::Type WriterPtr;
+    typedef std::vector<WriterPtr> WriterVector;
+
+    explicit MonolithicSimulator(Initializer<CELL> *initializer) : Simulator<CELL>(initializer) {}
+    virtual const typename Simulator<CELL>::GridType *getGrid() = 0;
+    virtual void addWriter(Writer<CELL> *writer) { writers.push_back(WriterPtr(writer)); }
+    std::vector<Chronometer> gatherStatistics() { return std::vector<Chronometer>(1, this->chronometer); }
+
+protected:
+    WriterVector writers;
+};
+
+}  // namespace LibGeoDecomp
+
+#endif

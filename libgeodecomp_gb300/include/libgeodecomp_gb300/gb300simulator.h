@@ -1,0 +1,270 @@
+// GB300Simulator<CELL>: drop-in for LibGeoDecomp's CUDASimulator<CELL>
+// (parallelization/cudasimulator.h:298-596) on top of the C ABI in
+// include/lgd_gpu.h.
+//
+// The Simulator / MonolithicSimulator surface, the plugin calls and their
+// order are those of the reference's single-node simulators
+// (parallelization/serialsimulator.h:48-180): Steerers run before a step
+// when stepNum % period == 0 (and with STEERER_INITIALIZED / ALL_DONE around
+// run()), Writers get WRITER_INITIALIZED at the start step,
+// WRITER_STEP_FINISHED when step % period == 0 and WRITER_ALL_DONE at
+// maxSteps; SteererFeedback::endSimulation() stops run(); startStep() is
+// honoured.  The simulator owns the Initializer, Writers and Steerers.
+//
+// Differences from CUDASimulator, all on the host <-> device path:
+//   - the grid is copied back to the host only when a Writer, a Steerer or
+//     getGrid() needs it (the reference copies the whole grid every time a
+//     writer asks, :490-497);
+//   - after Steerers ran, the host grid is uploaded again, so steering
+//     changes reach the device (the reference leaves this as a fixme,
+//     :450-454);
+//   - blockSize is accepted for signature compatibility and validated; the
+//     library picks its own launch shapes.
+//
+// Cells are bound to a kernel compiled into the library by specialising
+// GB300CellTraits<CELL> (see below); the cell class and its API traits stay
+// as they are.
+//
+// Build with -DLGD_GB300_WITH_REFERENCE and the reference's include paths to
+// plug into a LibGeoDecomp application; without it the declarations in
+// compat.h stand in for the reference's.
+#ifndef LGD_GB300_SIMULATOR_H
+#define LGD_GB300_SIMULATOR_H
+
+#ifdef LGD_GB300_WITH_REFERENCE
+#include <libgeodecomp/io/initializer.h>
+#include <libgeodecomp/io/steerer.h>
+#include <libgeodecomp/io/writer.h>
+#include <libgeodecomp/parallelization/monolithicsimulator.h>
+#include <libgeodecomp/storage/displacedgrid.h>
+#else
+#include "compat.h"
+#endif
+
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "lgd_gpu.h"
+
+namespace LibGeoDecomp {
+
+// Binding of a cell class to a cell kind of the GPU library.  A
+// specialisation provides
+//   static const int KIND;                        LGD_CELL_* of lgd_gpu.h
+//   static const int MEMBERS;                     SoA members, in the kind's order
+//   static std::size_t memberSize(int m);         bytes of member m
+//   static void pack(const CELL& c, int m, void *dst);     member m -> dst
+//   static void unpack(CELL *c, int m, const void *src);   src -> member m
+//   static double edgeValue(const CELL& c, int m);         member m as double
+template<typename CELL>
+class GB300CellTraits;
+
+// Maps a non-zero status of the C ABI to the exception the reference throws
+// in the same situation.
+inline void gb300Check(int rc)
+{
+    if (rc == LGD_OK) return;
+    char msg[512];
+    lgd_gpu_last_error(msg, sizeof(msg));
+    switch (rc) {
+    case LGD_ERR_INVALID:
+        throw std::invalid_argument(msg);
+    case LGD_ERR_RANGE:
+        throw std::out_of_range(msg);
+    case LGD_ERR_UNSUPPORTED:
+        throw std::logic_error(msg);
+    default:
+        throw std::runtime_error(std::string("CUDA error: ") + msg);
+    }
+}
+
+template<typename CELL>
+class GB300Simulator : public MonolithicSimulator<CELL> {
+public:
+    typedef typename APITraits::SelectTopology<CELL>::Value Topology;
+    static const int DIM = Topology::DIM;
+    static const unsigned NANO_STEPS = APITraits::SelectNanoSteps<CELL>::VALUE;
+    typedef GridBase<CELL, DIM> GridBaseType;
+    typedef DisplacedGrid<CELL, Topology> HostGrid;
+    typedef typename Steerer<CELL>::SteererFeedback SteererFeedback;
+    typedef GB300CellTraits<CELL> Traits;
+
+    explicit GB300Simulator(Initializer<CELL> *initializer, Coord<3> blockSize = Coord<3>(128, DIM < 3 ? 1 : 4, 1)) :
+        MonolithicSimulator<CELL>(initializer),
+        handle(0),
+        hostGrid(0),
+        hostStale(false)
+    {
+        if (blockSize.x() <= 0 || blockSize.y() <= 0 || blockSize.z() <= 0) {
+            throw std::invalid_argument("blockSize must be positive");
+        }
+        this->stepNum = initializer->startStep();
+        box = initializer->gridBox();
+        simArea << box;
+        hostGrid = new HostGrid(box);
+        initializer->grid(hostGrid);
+        createDevice();
+        upload();
+    }
+
+    virtual ~GB300Simulator()
+    {
+        if (handle) lgd_gpu_destroy(handle);
+        delete hostGrid;
+    }
+
+    virtual void step()
+    {
+        SteererFeedback feedback;
+        step(&feedback);
+    }
+
+    virtual void step(SteererFeedback *feedback)
+    {
+        handleInput(STEERER_NEXT_STEP, feedback);
+        for (unsigned i = 0; i < NANO_STEPS; ++i) {
+            gb300Check(lgd_gpu_step(handle, i, 1));
+        }
+        hostStale = true;
+        ++this->stepNum;
+        WriterEvent event = WRITER_STEP_FINISHED;
+        if (this->stepNum == this->initializer->maxSteps()) {
+            event = WRITER_ALL_DONE;
+        }
+        handleOutput(event);
+    }
+
+    virtual void run()
+    {
+        this->initializer->grid(hostGrid);
+        hostStale = false;
+        this->stepNum = this->initializer->startStep();
+        if (edgeChanged()) {
+            gb300Check(lgd_gpu_destroy(handle));
+            handle = 0;
+            createDevice();
+        }
+        upload();
+        for (std::size_t i = 0; i < this->steerers.size(); ++i) {
+            this->steerers[i]->setRegion(simArea);
+        }
+        SteererFeedback feedback;
+        handleInput(STEERER_INITIALIZED, &feedback);
+        handleOutput(WRITER_INITIALIZED);
+        while (this->stepNum < this->initializer->maxSteps()) {
+            if (feedback.simulationEnded()) break;
+            step(&feedback);
+        }
+        handleInput(STEERER_ALL_DONE, &feedback);
+    }
+
+    virtual const GridBaseType *getGrid()
+    {
+        download();
+        return hostGrid;
+    }
+
+    // The library handle, for callers that want the device grid directly.
+    lgd_handle *deviceHandle() { return handle; }
+
+private:
+    lgd_handle *handle;
+    HostGrid *hostGrid;
+    CoordBox<DIM> box;
+    Region<DIM> simArea;
+    bool hostStale;
+    double edge[4];
+
+    void createDevice()
+    {
+        lgd_grid_desc d;
+        std::memset(&d, 0, sizeof(d));
+        d.dim = DIM;
+        d.nx = box.dimensions[0];
+        d.ny = DIM > 1 ? box.dimensions[1] : 1;
+        d.nz = DIM > 2 ? box.dimensions[2] : 1;
+        d.periodic = (Topology::template WrapsAxis<0>::VALUE ? 1 : 0) |
+                     (Topology::template WrapsAxis<1>::VALUE ? 2 : 0) |
+                     (Topology::template WrapsAxis<2>::VALUE ? 4 : 0);
+        d.cell = Traits::KIND;
+        for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
+            d.edge[m] = Traits::edgeValue(hostGrid->getEdge(), m);
+            edge[m] = d.edge[m];
+        }
+        gb300Check(lgd_gpu_create(&d, &handle));
+    }
+
+    bool edgeChanged() const
+    {
+        for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
+            if (Traits::edgeValue(hostGrid->getEdge(), m) != edge[m]) return true;
+        }
+        return false;
+    }
+
+    // host grid -> dense member arrays -> device (current buffer)
+    void upload()
+    {
+        const std::size_t n = box.size();
+        std::vector<char> buf;
+        for (int m = 0; m < Traits::MEMBERS; ++m) {
+            const std::size_t sz = Traits::memberSize(m);
+            buf.resize(n * sz);
+            std::size_t i = 0;
+            for (typename CoordBox<DIM>::Iterator c = box.begin(); c != box.end(); ++c, ++i) {
+                Traits::pack(hostGrid->get(*c), m, &buf[i * sz]);
+            }
+            gb300Check(lgd_gpu_upload(handle, m, 0, buf.data(), buf.size()));
+        }
+        hostStale = false;
+    }
+
+    void download()
+    {
+        if (!hostStale) return;
+        const std::size_t n = box.size();
+        std::vector<std::vector<char> > bufs(Traits::MEMBERS);
+        for (int m = 0; m < Traits::MEMBERS; ++m) {
+            bufs[m].resize(n * Traits::memberSize(m));
+            gb300Check(lgd_gpu_download(handle, m, 0, bufs[m].data(), bufs[m].size()));
+        }
+        std::size_t i = 0;
+        for (typename CoordBox<DIM>::Iterator c = box.begin(); c != box.end(); ++c, ++i) {
+            CELL cell = hostGrid->get(*c);
+            for (int m = 0; m < Traits::MEMBERS; ++m) {
+                Traits::unpack(&cell, m, &bufs[m][i * Traits::memberSize(m)]);
+            }
+            hostGrid->set(*c, cell);
+        }
+        hostStale = false;
+    }
+
+    void handleInput(SteererEvent event, SteererFeedback *feedback)
+    {
+        bool called = false;
+        for (std::size_t i = 0; i < this->steerers.size(); ++i) {
+            if ((event != STEERER_NEXT_STEP) || (this->stepNum % this->steerers[i]->getPeriod() == 0)) {
+                if (!called) download();
+                called = true;
+                this->steerers[i]->nextStep(hostGrid, simArea, this->gridDim, this->getStep(), event, 0, true,
+                                            feedback);
+            }
+        }
+        if (called) upload();   // steering changes reach the device
+    }
+
+    void handleOutput(WriterEvent event)
+    {
+        for (std::size_t i = 0; i < this->writers.size(); ++i) {
+            if ((event != WRITER_STEP_FINISHED) || ((this->getStep() % this->writers[i]->getPeriod()) == 0)) {
+                this->writers[i]->stepFinished(*getGrid(), this->getStep(), event);
+            }
+        }
+    }
+};
+
+}  // namespace LibGeoDecomp
+
+#endif

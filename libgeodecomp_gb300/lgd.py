@@ -102,6 +102,20 @@ def lib():
             "lgd_sell_synchronize": [P],
             "lgd_sell_stream": [P, P],
             "lgd_sell_launch_count": [P, P],
+            "lgd_lbm_create": [I, P, P, ctypes.c_double, I, P],
+            "lgd_lbm_destroy": [P],
+            "lgd_lbm_step": [P, I],
+            "lgd_lbm_step_looped": [P, I],
+            "lgd_lbm_set_config": [P, I, I, I],
+            "lgd_lbm_get_config": [P, P, P, P],
+            "lgd_lbm_tune": [P, I, P, P, P, P],
+            "lgd_lbm_reset": [P],
+            "lgd_lbm_download": [P, I, P, S],
+            "lgd_lbm_upload": [P, I, P, S],
+            "lgd_lbm_info": [P, P, P],
+            "lgd_lbm_synchronize": [P],
+            "lgd_lbm_stream": [P, P],
+            "lgd_lbm_launch_count": [P, P],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -325,4 +339,84 @@ class SellGrid:
     def launch_count(self) -> int:
         n = ctypes.c_uint64()
         check(lib().lgd_sell_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+
+# ------------------------------------------------------------ LBM ensemble
+class LbmEnsemble:
+    """Ensemble of D3Q19 lid-driven cavities (include/lgd_ensemble.h)."""
+
+    def __init__(self, edges, omegas, lid: float = 0.05, precision: int = 4):
+        self.edges = np.ascontiguousarray(edges, dtype=np.int32)
+        self.omegas = np.ascontiguousarray(omegas, dtype=np.float64)
+        self._h = ctypes.c_void_p()
+        check(lib().lgd_lbm_create(len(self.edges), _ptr(self.edges), _ptr(self.omegas), float(lid), precision,
+                                   ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            check(lib().lgd_lbm_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, steps: int = 1):
+        check(lib().lgd_lbm_step(self._h, steps))
+
+    def step_looped(self, steps: int = 1):
+        check(lib().lgd_lbm_step_looped(self._h, steps))
+
+    def set_config(self, tile_rows: int, threads: int, ctas_per_sm: int):
+        check(lib().lgd_lbm_set_config(self._h, tile_rows, threads, ctas_per_sm))
+
+    def config(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().lgd_lbm_get_config(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def tune(self, trial_steps: int = 4):
+        a, b, c, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        check(lib().lgd_lbm_tune(self._h, trial_steps, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                 ctypes.byref(t)))
+        return (a.value, b.value, c.value), t.value
+
+    def reset(self):
+        check(lib().lgd_lbm_reset(self._h))
+
+    def download(self, instance: int) -> np.ndarray:
+        L = int(self.edges[instance])
+        out = np.empty((19, L, L, L), dtype=np.float64)
+        check(lib().lgd_lbm_download(self._h, instance, _ptr(out), out.nbytes))
+        return out
+
+    def upload(self, instance: int, f: np.ndarray):
+        a = np.ascontiguousarray(f, dtype=np.float64)
+        check(lib().lgd_lbm_upload(self._h, instance, _ptr(a), a.nbytes))
+
+    def info(self):
+        c, n = ctypes.c_longlong(), ctypes.c_int()
+        check(lib().lgd_lbm_info(self._h, ctypes.byref(c), ctypes.byref(n)))
+        return c.value, n.value
+
+    def synchronize(self):
+        check(lib().lgd_lbm_synchronize(self._h))
+
+    def stream(self) -> int:
+        p = ctypes.c_void_p()
+        check(lib().lgd_lbm_stream(self._h, ctypes.byref(p)))
+        return p.value
+
+    def launch_count(self) -> int:
+        n = ctypes.c_uint64()
+        check(lib().lgd_lbm_launch_count(self._h, ctypes.byref(n)))
         return n.value

@@ -56,6 +56,7 @@ def lib():
         D = ctypes.c_double
         L.lgd_oracle_max_threads.restype = I
         L.lgd_oracle_jacobi7.argtypes = [I, I, I, I, D, I, P, I]
+        L.lgd_oracle_jacobi7_pp.argtypes = [I, I, I, I, D, I, P, P, I]
         L.lgd_oracle_gol.argtypes = [I, I, I, P, I]
         L.lgd_oracle_sell_plan.argtypes = [I, P, I, I, P, P, P, P]
         L.lgd_oracle_sell_plan.restype = ctypes.c_longlong
@@ -83,6 +84,23 @@ def jacobi7(u: np.ndarray, steps: int, torus: bool = False, edge: float = 0.0, t
     rc = lib().lgd_oracle_jacobi7(nx, ny, nz, int(torus), float(edge), int(steps), _ptr(out), threads)
     assert rc == 0
     return out
+
+
+class Jacobi7PingPong:
+    """Jacobi-7 state with two preallocated buffers, for timing whole steps
+    without allocation or copies."""
+
+    def __init__(self, u: np.ndarray, torus: bool = False, edge: float = 0.0, threads: int = 0):
+        self.a = np.ascontiguousarray(u, dtype=np.float64).copy()
+        self.b = np.empty_like(self.a)
+        self.torus, self.edge, self.threads = int(torus), float(edge), threads
+
+    def step(self, steps: int) -> "Jacobi7PingPong":
+        nz, ny, nx = self.a.shape
+        if lib().lgd_oracle_jacobi7_pp(nx, ny, nz, self.torus, self.edge, int(steps), _ptr(self.a), _ptr(self.b),
+                                       self.threads):
+            self.a, self.b = self.b, self.a
+        return self
 
 
 def gol(cells: np.ndarray, steps: int, threads: int = 0) -> np.ndarray:

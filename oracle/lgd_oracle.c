@@ -114,6 +114,22 @@ int lgd_oracle_jacobi7(int nx, int ny, int nz, int torus, double edge, int steps
     return 0;
 }
 
+/* Ping-pong form for timing: steps time steps between caller-owned buffers
+ * a (input) and b, no allocation; returns 0 if the result is in a, 1 if in b. */
+int lgd_oracle_jacobi7_pp(int nx, int ny, int nz, int torus, double edge, int steps,
+                          double *a, double *b, int threads)
+{
+    set_threads(threads);
+    for (int s = 0; s < steps; ++s) {
+        if (s % 2 == 0) {
+            jacobi7_step(nx, ny, nz, torus, edge, a, b);
+        } else {
+            jacobi7_step(nx, ny, nz, torus, edge, b, a);
+        }
+    }
+    return steps % 2;
+}
+
 /* -------------------------------------------------------------- Game of Life
  * Reference: ConwayCell::update (src/examples/gameoflife/main.cpp:35-58) with
  * uint8 cells on a torus, run by VanillaUpdateFunctor

@@ -1,0 +1,314 @@
+// Conformance test of GB300Simulator<CELL> (drop-in for CUDASimulator) with
+// unchanged Initializer / Writer / Steerer plugins.  Mirrors what the
+// reference's SerialSimulator and CUDASimulator tests check
+// (parallelization/test/unit/serialsimulatortest.h,
+// parallelization/test/unit/cudasimulatortest.h:66-238, io/testwriter.h:40-62):
+// the event sequence, steering, startStep, the result grid.  Expected grids
+// come from a plain CPU loop over the same cell rule.
+//
+// Builds against include/lgd_gpu.h + libgeodecomp_gb300/include (compat
+// declarations) or, with -DLGD_GB300_WITH_REFERENCE, against the reference.
+#include <libgeodecomp_gb300/gb300simulator.h>
+#ifdef LGD_GB300_WITH_REFERENCE
+#include <libgeodecomp/io/simpleinitializer.h>
+#endif
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+using namespace LibGeoDecomp;
+
+static int failures = 0;
+#define EXPECT(cond)                                                          \
+    do {                                                                      \
+        if (!(cond)) {                                                        \
+            std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #cond);    \
+            ++failures;                                                       \
+        }                                                                     \
+    } while (0)
+
+// ------------------------------------------------------------ Jacobi cell
+class JacobiCell {
+public:
+    class API : public APITraits::HasCubeTopology<3>,
+                public APITraits::HasStencil<Stencils::VonNeumann<3, 1> >,
+                public APITraits::HasFixedCoordsOnlyUpdate,
+                public APITraits::HasUpdateLineX {};
+
+    explicit JacobiCell(double v = 0) : temp(v) {}
+    double temp;
+};
+
+namespace LibGeoDecomp {
+template<>
+class GB300CellTraits<JacobiCell> {
+public:
+    static const int KIND = LGD_CELL_JACOBI7_F64;
+    static const int MEMBERS = 1;
+    static std::size_t memberSize(int) { return sizeof(double); }
+    static void pack(const JacobiCell& c, int, void *dst) { std::memcpy(dst, &c.temp, sizeof(double)); }
+    static void unpack(JacobiCell *c, int, const void *src) { std::memcpy(&c->temp, src, sizeof(double)); }
+    static double edgeValue(const JacobiCell& c, int) { return c.temp; }
+};
+}
+
+static double initialValue(int x, int y, int z)
+{
+    return std::fmod(0.37 * x + 0.11 * y * y + 0.071 * z + 0.013 * x * z, 1.0);
+}
+
+class JacobiInit : public SimpleInitializer<JacobiCell> {
+public:
+    JacobiInit(Coord<3> dim, unsigned steps, unsigned start = 0) :
+        SimpleInitializer<JacobiCell>(dim, steps), start(start)
+    {}
+
+    virtual void grid(GridBase<JacobiCell, 3> *ret)
+    {
+        CoordBox<3> box = ret->boundingBox();
+        for (CoordBox<3>::Iterator i = box.begin(); i != box.end(); ++i) {
+            ret->set(*i, JacobiCell(initialValue(i->x(), i->y(), i->z())));
+        }
+        ret->setEdge(JacobiCell(0.25));
+    }
+
+    unsigned startStep() const { return start; }
+
+private:
+    unsigned start;
+};
+
+// CPU reference of the Jacobi rule with edge value 0.25
+static std::vector<double> cpuJacobi(Coord<3> d, int steps)
+{
+    const int nx = d.x(), ny = d.y(), nz = d.z();
+    std::vector<double> a((std::size_t)nx * ny * nz), b(a.size());
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) a[((std::size_t)z * ny + y) * nx + x] = initialValue(x, y, z);
+    auto at = [&](const std::vector<double>& v, int x, int y, int z) {
+        if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0.25;
+        return v[((std::size_t)z * ny + y) * nx + x];
+    };
+    for (int s = 0; s < steps; ++s) {
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y)
+                for (int x = 0; x < nx; ++x) {
+                    volatile double acc = at(a, x, y, z);
+                    acc = acc + at(a, x, y - 1, z);
+                    acc = acc + at(a, x, y + 1, z);
+                    acc = acc + at(a, x + 1, y, z);
+                    acc = acc + at(a, x - 1, y, z);
+                    acc = acc + at(a, x, y, z + 1);
+                    acc = acc + at(a, x, y, z - 1);
+                    b[((std::size_t)z * ny + y) * nx + x] = acc * (1.0 / 7.0);
+                }
+        a.swap(b);
+    }
+    return a;
+}
+
+struct Event {
+    unsigned step;
+    int event;
+    double sum;
+};
+
+class RecordingWriter : public Writer<JacobiCell> {
+public:
+    RecordingWriter(unsigned period, std::vector<Event> *log) : Writer<JacobiCell>("rec", period), log(log) {}
+    Writer<JacobiCell> *clone() const { return new RecordingWriter(period, log); }
+
+    void stepFinished(const GridType& grid, unsigned step, WriterEvent event)
+    {
+        double s = 0;
+        CoordBox<3> box = grid.boundingBox();
+        for (CoordBox<3>::Iterator i = box.begin(); i != box.end(); ++i) s += grid.get(*i).temp;
+        log->push_back(Event{step, (int)event, s});
+    }
+
+private:
+    std::vector<Event> *log;
+};
+
+class StopSteerer : public Steerer<JacobiCell> {
+public:
+    StopSteerer(unsigned period, unsigned stopAt, std::vector<Event> *log) :
+        Steerer<JacobiCell>(period), stopAt(stopAt), log(log)
+    {}
+
+    void nextStep(GridType *grid, const Region<3>&, const Coord<3>&, unsigned step, SteererEvent event, std::size_t,
+                  bool, SteererFeedback *feedback)
+    {
+        log->push_back(Event{step, 100 + (int)event, 0.0});
+        if (event == STEERER_NEXT_STEP && step >= stopAt) feedback->endSimulation();
+        (void)grid;
+    }
+
+private:
+    unsigned stopAt;
+    std::vector<Event> *log;
+};
+
+// sets one cell every time it runs: the change must reach the device
+class PokeSteerer : public Steerer<JacobiCell> {
+public:
+    explicit PokeSteerer(unsigned period) : Steerer<JacobiCell>(period) {}
+    void nextStep(GridType *grid, const Region<3>&, const Coord<3>&, unsigned, SteererEvent event, std::size_t, bool,
+                  SteererFeedback *)
+    {
+        if (event == STEERER_NEXT_STEP) grid->set(Coord<3>(1, 2, 3), JacobiCell(1000.0));
+    }
+};
+
+static void testRunEventsAndResult()
+{
+    const Coord<3> dim(21, 13, 9);
+    std::vector<Event> log;
+    GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 12));
+    sim.addWriter(new RecordingWriter(5, &log));
+    sim.run();
+    EXPECT(sim.getStep() == 12);
+    // INITIALIZED@0, STEP_FINISHED@5, @10, ALL_DONE@12
+    EXPECT(log.size() == 4);
+    if (log.size() == 4) {
+        EXPECT(log[0].step == 0 && log[0].event == WRITER_INITIALIZED);
+        EXPECT(log[1].step == 5 && log[1].event == WRITER_STEP_FINISHED);
+        EXPECT(log[2].step == 10 && log[2].event == WRITER_STEP_FINISHED);
+        EXPECT(log[3].step == 12 && log[3].event == WRITER_ALL_DONE);
+    }
+    std::vector<double> ref = cpuJacobi(dim, 12);
+    const GridBase<JacobiCell, 3> *g = sim.getGrid();
+    std::size_t i = 0;
+    int mismatches = 0;
+    for (int z = 0; z < dim.z(); ++z)
+        for (int y = 0; y < dim.y(); ++y)
+            for (int x = 0; x < dim.x(); ++x, ++i) {
+                if (g->get(Coord<3>(x, y, z)).temp != ref[i]) ++mismatches;
+            }
+    EXPECT(mismatches == 0);
+}
+
+static void testSteererEndsRunAndStartStep()
+{
+    const Coord<3> dim(8, 7, 6);
+    std::vector<Event> log;
+    GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 40, 28));
+    sim.addSteerer(new StopSteerer(1, 33, &log));
+    sim.run();
+    // steps 28..32 run, the steerer asks to stop before step 33 runs
+    EXPECT(sim.getStep() == 34);
+    EXPECT(!log.empty() && log.front().event == 100 + STEERER_INITIALIZED && log.front().step == 28);
+    EXPECT(!log.empty() && log.back().event == 100 + STEERER_ALL_DONE);
+}
+
+static void testSteeringReachesDevice()
+{
+    const Coord<3> dim(6, 6, 6);
+    GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 3));
+    sim.addSteerer(new PokeSteerer(1));
+    sim.step();
+    // the poke happened before the step: the neighbours of (1,2,3) see it
+    const double n = sim.getGrid()->get(Coord<3>(2, 2, 3)).temp;
+    EXPECT(n > 100.0);
+}
+
+static void testManualStepsMatchCpu()
+{
+    const Coord<3> dim(17, 5, 11);
+    GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 100));
+    for (int s = 0; s < 7; ++s) sim.step();
+    std::vector<double> ref = cpuJacobi(dim, 7);
+    const GridBase<JacobiCell, 3> *g = sim.getGrid();
+    std::size_t i = 0;
+    int mismatches = 0;
+    for (int z = 0; z < dim.z(); ++z)
+        for (int y = 0; y < dim.y(); ++y)
+            for (int x = 0; x < dim.x(); ++x, ++i) mismatches += (g->get(Coord<3>(x, y, z)).temp != ref[i]);
+    EXPECT(mismatches == 0);
+    EXPECT(sim.getStep() == 7);
+}
+
+static void testBadBlockSizeThrows()
+{
+    bool thrown = false;
+    try {
+        GB300Simulator<JacobiCell> sim(new JacobiInit(Coord<3>(4, 4, 4), 1), Coord<3>(0, 1, 1));
+    } catch (const std::invalid_argument&) {
+        thrown = true;
+    }
+    EXPECT(thrown);
+}
+
+// ----------------------------------------------------- Game of Life (2D torus)
+class LifeCell {
+public:
+    class API : public APITraits::HasTorusTopology<2>, public APITraits::HasStencil<Stencils::Moore<2, 1> > {};
+    explicit LifeCell(unsigned char a = 0) : alive(a) {}
+    unsigned char alive;
+};
+
+namespace LibGeoDecomp {
+template<>
+class GB300CellTraits<LifeCell> {
+public:
+    static const int KIND = LGD_CELL_GOL_U8;
+    static const int MEMBERS = 1;
+    static std::size_t memberSize(int) { return 1; }
+    static void pack(const LifeCell& c, int, void *dst) { *(unsigned char *)dst = c.alive; }
+    static void unpack(LifeCell *c, int, const void *src) { c->alive = *(const unsigned char *)src; }
+    static double edgeValue(const LifeCell& c, int) { return c.alive; }
+};
+}
+
+class GliderInit : public SimpleInitializer<LifeCell> {
+public:
+    GliderInit() : SimpleInitializer<LifeCell>(Coord<2>(37, 29), 4 * 37) {}
+    virtual void grid(GridBase<LifeCell, 2> *ret)
+    {
+        const int g[5][2] = {{1, 0}, {2, 1}, {0, 2}, {1, 2}, {2, 2}};
+        for (int i = 0; i < 5; ++i) ret->set(Coord<2>(g[i][0] + 3, g[i][1] + 4), LifeCell(1));
+    }
+};
+
+static void testGliderCrossesTorus()
+{
+    // a glider moves (1, 1) every 4 generations; after 4 * 37 * 29 / gcd...
+    // use 4 * 37 generations: it moves 37 cells in x (one full turn) and 37
+    // in y (= 8 mod 29)
+    GB300Simulator<LifeCell> sim(new GliderInit());
+    sim.run();
+    const GridBase<LifeCell, 2> *g = sim.getGrid();
+    const int gl[5][2] = {{1, 0}, {2, 1}, {0, 2}, {1, 2}, {2, 2}};
+    int alive = 0, onGlider = 0;
+    CoordBox<2> box = g->boundingBox();
+    for (CoordBox<2>::Iterator i = box.begin(); i != box.end(); ++i) alive += g->get(*i).alive;
+    for (int i = 0; i < 5; ++i) {
+        onGlider += g->get(Coord<2>((gl[i][0] + 3 + 37) % 37, (gl[i][1] + 4 + 37) % 29)).alive;
+    }
+    EXPECT(alive == 5);
+    EXPECT(onGlider == 5);
+}
+
+int main()
+{
+    int n = 0;
+    if (lgd_gpu_device_count(&n) != LGD_OK || n == 0) {
+        std::printf("no GPU\n");
+        return 2;
+    }
+    testRunEventsAndResult();
+    testSteererEndsRunAndStartStep();
+    testSteeringReachesDevice();
+    testManualStepsMatchCpu();
+    testBadBlockSizeThrows();
+    testGliderCrossesTorus();
+    if (failures) {
+        std::printf("%d failure(s)\n", failures);
+        return 1;
+    }
+    std::printf("OK\n");
+    return 0;
+}

@@ -1,0 +1,95 @@
+"""D3Q19 ensemble on the GPU.  FP64 instances must match the reference's
+SerialSimulator (fixtures from tests/golden/gen_golden.py) within 1e-12 -
+in fact bit for bit, the kernel uses the oracle's operation order without
+fused multiply-adds; FP32 instances state their error against FP64."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from libgeodecomp_gb300 import lgd, workloads
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name + ".npz"), allow_pickle=False)
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_lbm_fp64_bit_exact_against_reference_L8():
+    g = load("lbm_L8")
+    with lgd.LbmEnsemble([int(g["L"])], [float(g["omega"])], lid=float(g["lid"]), precision=8) as e:
+        e.step(int(g["steps"]))
+        out = e.download(0)
+    np.testing.assert_array_equal(out, g["out"])
+
+
+def test_lbm_fp64_L24_golden():
+    g = load("lbm_L24")
+    with lgd.LbmEnsemble([int(g["L"])], [float(g["omega"])], lid=float(g["lid"]), precision=8) as e:
+        e.step(int(g["steps"]))
+        out = e.download(0)
+    np.testing.assert_array_equal(out.reshape(-1)[g["sample_idx"]], g["sample"])
+    assert sha(out) == str(g["sha256"])
+
+
+@pytest.mark.parametrize("config", [(1, 128, 1), (3, 64, 2), (16, 512, 1), (4, 256, 8)])
+def test_lbm_ensemble_uneven_sizes_match_oracle_any_launch_shape(config):
+    edges = [5, 12, 2, 9, 17, 3]
+    omegas = [1.0, 1.3, 1.9, 0.7, 1.55, 1.2]
+    with lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=8) as e:
+        e.set_config(*config)
+        e.step(11)
+        for j, (L, om) in enumerate(zip(edges, omegas)):
+            np.testing.assert_array_equal(e.download(j), oracle.lbm(L, 11, om, 0.05), err_msg=str(j))
+
+
+def test_lbm_persistent_equals_looped_launches():
+    edges, omegas = workloads.lbm_ensemble(12, seed=3, edge_min=4, edge_max=20)
+    with lgd.LbmEnsemble(edges, omegas, precision=4) as a, lgd.LbmEnsemble(edges, omegas, precision=4) as b:
+        a.step(7)
+        b.step_looped(7)
+        for j in range(len(edges)):
+            np.testing.assert_array_equal(a.download(j), b.download(j))
+
+
+def test_lbm_tuner_picks_a_valid_shape_and_reset_restores_rest_state():
+    edges, omegas = workloads.lbm_ensemble(16, seed=4, edge_min=8, edge_max=24)
+    with lgd.LbmEnsemble(edges, omegas, precision=4) as e:
+        (ty, th, ct), ms = e.tune(trial_steps=2)
+        assert ty >= 1 and th in (128, 256, 512) and ct >= 1 and ms > 0
+        e.reset()
+        e.step(5)
+        got = e.download(3)
+    ref = oracle.lbm(int(edges[3]), 5, float(omegas[3]), 0.05)
+    assert np.max(np.abs(got - ref)) < 1e-6
+
+
+def test_lbm_fp32_error_against_fp64():
+    L, om = 32, 1.7
+    with lgd.LbmEnsemble([L], [om], precision=4) as e:
+        e.step(200)
+        f32 = e.download(0)
+    f64 = oracle.lbm(L, 200, om, 0.05)
+    rel_l2 = np.linalg.norm(f32 - f64) / np.linalg.norm(f64)
+    max_abs = np.max(np.abs(f32 - f64))
+    assert rel_l2 < 1e-5 and max_abs < 1e-5, (rel_l2, max_abs)
+
+
+def test_lbm_upload_roundtrip_and_errors():
+    with lgd.LbmEnsemble([6, 4], [1.2, 1.5], precision=8) as e:
+        f = np.random.default_rng(0).random((19, 4, 4, 4))
+        e.upload(1, f)
+        np.testing.assert_array_equal(e.download(1), f)
+        with pytest.raises(lgd.LGDError) as err:
+            e.download(2)
+        assert err.value.code == lgd.ERR_RANGE
+    with pytest.raises(lgd.LGDError):
+        lgd.LbmEnsemble([4], [2.5])

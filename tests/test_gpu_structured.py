@@ -99,7 +99,9 @@ def test_jacobi7_fixed_point_signed_values_and_edge():
     # reference itself rounds each of its 7 operations per step (ulp(2.4) =
     # 4.4e-16), so the difference is dominated by the reference's own rounding
     assert np.max(np.abs(out - ref)) <= 20 * 7 * 4.5e-16
-    assert rel_err(out, ref) <= 1e-12
+    # relative error is meaningful away from the values that cross zero
+    mask = np.abs(ref) > 1e-3
+    assert rel_err(out[mask], ref[mask]) <= 1e-12
 
 
 def test_jacobi7_fixed_point_device_fill_matches_host_generator():
