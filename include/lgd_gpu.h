@@ -160,6 +160,25 @@ int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
  * order their own work against the library's. */
 int lgd_gpu_stream(lgd_handle *h, void **stream);
 
+/* ------------------------------------------------- allocation-free sum
+ * No counterpart in the reference.  Sum of n FP64 values in device memory,
+ * written to *d_result (device memory), asynchronously on stream (a
+ * cudaStream_t, NULL = the default stream) - the same reduction as
+ * lgd_gpu_checksum, for callers that must not allocate device memory: a
+ * plugin or solver running inside another framework's stream and memory
+ * pool, where cudaMalloc/cudaFree would synchronise the device and
+ * fragment the pool, or code with a fixed memory budget.  It calls no
+ * allocating routine: its block partials live in a fixed 128 KiB device
+ * array that every GPU loading the library keeps until the process exits.
+ * Hence n <= LGD_SUM_STATIC_MAX_N (larger n returns LGD_ERR_RANGE), and
+ * calls that overlap on the GPU (unordered streams) race on that array.
+ * The first call on a device looks the array's address up (no
+ * allocation); make that first call before any stream capture. */
+#define LGD_SUM_STATIC_CHUNK 65536
+#define LGD_SUM_STATIC_MAX_PARTIALS 16384
+#define LGD_SUM_STATIC_MAX_N (1LL << 30)
+int lgd_sum_f64_static(const double *d_values, long long n, double *d_result, void *stream);
+
 /* Sum of one member over the whole grid in FP64 (deterministic order). */
 int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum);
 
