@@ -127,15 +127,15 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- workloads
 class JacobiWorkload:
-    shape = (512, 512, 512)
     run_steps = 100
     bytes_per_unit = 16          # one FP64 read + one FP64 write per cell and step
 
-    def __init__(self, ieee: bool):
+    def __init__(self, ieee: bool, edge: int = 512):
         from libgeodecomp_gb300 import lgd, workloads
+        self.shape = (edge, edge, edge)
         self.lgd = lgd
         self.ieee = ieee
-        self.name = "jacobi7_f64_ieee_512" if ieee else "jacobi7_f64_512"
+        self.name = ("jacobi7_f64_ieee_%d" if ieee else "jacobi7_f64_%d") % edge
         self.metric = JACOBI_METRIC
         self.unit = "GLUPS"
         self.units = int(np.prod(self.shape))
@@ -144,7 +144,8 @@ class JacobiWorkload:
         self.g = lgd.Grid(cell, self.shape, periodic=0)
         self.g.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
         self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "constant 0",
-                       "cells": self.units, "l2": "inputs larger than L2 (1 GiB per buffer)",
+                       "cells": self.units,
+                       "l2": "inputs larger than L2 (%d MiB per buffer)" % (self.units * 8 >> 20),
                        "cell_update": "(c+n+s+e+w+t+b)*(1/7)"}
 
     def stream(self):
@@ -266,11 +267,11 @@ class SellWorkload:
         self.g.close()
 
 
-def make_workload(name):
+def make_workload(name, size=512):
     if name == "jacobi7_f64_512":
-        return JacobiWorkload(ieee=False)
+        return JacobiWorkload(ieee=False, edge=size)
     if name == "jacobi7_f64_ieee_512":
-        return JacobiWorkload(ieee=True)
+        return JacobiWorkload(ieee=True, edge=size)
     if name == "gol_u8_8192":
         return GoLWorkload()
     if name == "sell_f64_4m":
@@ -322,7 +323,7 @@ def time_steps(torch, w, steps):
 def run_gpu(args, world, rank, local, dist):
     import torch
     torch.cuda.set_device(local)
-    w = make_workload(args.workload)
+    w = make_workload(args.workload, args.size)
     for _ in range(args.warmup):
         w.step(1)
     w.sync()
@@ -369,7 +370,7 @@ def run_gpu(args, world, rank, local, dist):
     extra = {}
     if args.workload == "jacobi7_f64_512" and not args.no_ieee:
         w.close()
-        wi = make_workload("jacobi7_f64_ieee_512")
+        wi = make_workload("jacobi7_f64_ieee_512", args.size)
         for _ in range(3):
             wi.step(1)
         wi.sync()
@@ -476,6 +477,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=WORKLOAD_NAMES, default="jacobi7_f64_512")
     ap.add_argument("--e2e-runs", type=int, default=2)
+    ap.add_argument("--size", type=int, default=512, help="cube edge of the Jacobi workloads (small profiling cases)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ieee", action="store_true")

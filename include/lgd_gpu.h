@@ -60,11 +60,11 @@ int lgd_gpu_device_count(int *count);
  *                          bit-identical to the reference's SerialSimulator)
  *   LGD_CELL_JACOBI7_F64_FIX same cell with FP64 values at the ABI; on the
  *                          device the grid is held in 64-bit fixed point,
- *                          value = k * 2^(e - 60) with e the smallest power
+ *                          value = k * 2^(e - 59) with 2^e the smallest power
  *                          of two above every value uploaded so far and the
  *                          edge cell.  The neighbour sum is exact and the
  *                          division by 7 rounds to the nearest unit, so each
- *                          step adds at most 2^(e - 61) absolute error.  For
+ *                          step adds at most 2^(e - 60) absolute error.  For
  *                          GPUs whose FP64 pipe, not memory, would bound the
  *                          IEEE kernel.
  *   LGD_CELL_JACOBI7_F32   members {float temp}; same stencil in FP32
@@ -155,6 +155,11 @@ int lgd_gpu_fill_bernoulli(lgd_handle *h, int member, int which, uint64_t seed, 
 
 /* Fixed-point exponent e of an LGD_CELL_JACOBI7_F64_FIX grid. */
 int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
+
+/* Kernel variant for the Jacobi cells (results are identical): 0 (default)
+ * register columns marching in z with warp shuffles for x-neighbours, 1
+ * shared-memory plane tiles.  For tuning and comparison. */
+int lgd_gpu_set_variant(lgd_handle *h, int variant);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or
  * order their own work against the library's. */

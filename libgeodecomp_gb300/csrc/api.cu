@@ -50,7 +50,7 @@ static CellInfo cell_info(int cell)
 }
 
 // ---------------------------------------------------------- fixed point
-// The FP64 Jacobi grid in fixed-point form: value = k * 2^(fix_exp - 60).
+// The FP64 Jacobi grid in fixed-point form: value = k * 2^(fix_exp - LGD_FIX_BITS).
 // fix_exp is chosen at upload so that every value and the edge cell fit
 // (|value| <= 2^fix_exp); averaging never leaves that range.
 static int exp_bound(double m)
@@ -64,7 +64,7 @@ static int exp_bound(double m)
 
 long long fix_edge(const Grid& g)
 {
-    return std::llrint(std::ldexp(g.desc.edge[0], 60 - g.fix_exp));
+    return std::llrint(std::ldexp(g.desc.edge[0], LGD_FIX_BITS - g.fix_exp));
 }
 
 int fix_scale_exp(const Grid& g)
@@ -79,7 +79,7 @@ __global__ void to_fix_pitched_kernel(const double *src, long long *dst, int nx,
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const long long r = i / nx;
         const long long x = i - r * nx;
-        dst[r * pitch + x] = __double2ll_rn(ldexp(src[i], 60 - exp));
+        dst[r * pitch + x] = __double2ll_rn(ldexp(src[i], LGD_FIX_BITS - exp));
     }
 }
 
@@ -89,7 +89,7 @@ __global__ void from_fix_pitched_kernel(const long long *src, double *dst, int n
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const long long r = i / nx;
         const long long x = i - r * nx;
-        dst[i] = ldexp((double)src[r * pitch + x], exp - 60);
+        dst[i] = ldexp((double)src[r * pitch + x], exp - LGD_FIX_BITS);
     }
 }
 
@@ -568,6 +568,15 @@ int lgd_gpu_set_time_block(lgd_handle *h, int depth)
         Grid& g = grid_of(h);
         LGD_REQUIRE(depth >= 0 && depth <= 64, LGD_ERR_INVALID, "time block depth out of range");
         g.time_block = depth;
+    });
+}
+
+int lgd_gpu_set_variant(lgd_handle *h, int variant)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(variant == 0 || variant == 1, LGD_ERR_INVALID, "variant must be 0 or 1");
+        g.variant = variant;
     });
 }
 

@@ -59,18 +59,22 @@ __host__ __device__ __forceinline__ double splitmix_uniform(uint64_t key, uint64
 }
 
 // ---- fixed-point representation of the FP64 Jacobi grid
-// value = k * 2^(scale_exp - 60), k a signed 64-bit integer, |value| <= 2^scale_exp.
-// The averaging stencil maps [-S, S] into itself, so 7 * 2^60 bounds every
-// neighbour sum and nothing overflows.
+// value = k * 2^(scale_exp - LGD_FIX_BITS), k a signed 64-bit integer,
+// |value| < 2^scale_exp, so |k| < 2^59.  The averaging stencil maps
+// [-S, S] into itself, so 7 * 2^59 bounds every neighbour sum and nothing
+// overflows.
+#define LGD_FIX_BITS 59
+
 __device__ __forceinline__ long long fx_div7_round(long long sum)
 {
-    // round(sum / 7) with ties towards +inf, via an unsigned offset so that
-    // the division is a multiply-high (sum is in [-7*2^60, 7*2^60]).
-    const unsigned long long off = 7ull << 60;
-    unsigned long long n = (unsigned long long)(sum + 3) + off;
-    unsigned long long t = __umul64hi(n, 0x2492492492492493ull);
-    unsigned long long q = (((n - t) >> 1) + t) >> 2;
-    return (long long)(q - (1ull << 60));
+    // round(sum / 7) (no ties exist), via an unsigned offset so that the
+    // division is one multiply-high: for n < 7 * 2^60 + 3,
+    // floor(n / 7) = floor(n * ceil(2^65 / 7) / 2^65) exactly (the error
+    // term n * (3/7) / 2^65 stays below 1/7).
+    const unsigned long long off = 7ull << 59;
+    const unsigned long long n = (unsigned long long)(sum + 3) + off;
+    const unsigned long long q = __umul64hi(n, 0x4924924924924925ull) >> 1;
+    return (long long)(q - (1ull << 59));
 }
 
 }  // namespace lgd

@@ -243,7 +243,7 @@ __global__ void fill_kernel(View<T> v, uint64_t key, double p, int scale_exp)
         } else if (MODE == 1) {
             v.at(x, y, z) = (T)(u < p ? 1 : 0);
         } else {
-            v.at(x, y, z) = (T)__double2ll_rn(ldexp(u, 60 - scale_exp));
+            v.at(x, y, z) = (T)__double2ll_rn(ldexp(u, LGD_FIX_BITS - scale_exp));
         }
     }
 }
@@ -291,7 +291,7 @@ __global__ void checksum_kernel(View<const T> v, double *partials, int scale_exp
     for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
         const T *row = v.p + r * v.pitch;
         for (int x = threadIdx.x; x < v.nx; x += blockDim.x) {
-            acc += FIX ? ldexp((double)row[x], scale_exp - 60) : (double)row[x];
+            acc += FIX ? ldexp((double)row[x], scale_exp - LGD_FIX_BITS) : (double)row[x];
         }
     }
     red[threadIdx.x] = acc;

@@ -71,6 +71,74 @@ jacobi7_zmarch_kernel(View<const typename CELL::T> in, View<typename CELL::T> ou
     }
 }
 
+// Register-column variant: a warp owns 32 consecutive x and TY consecutive
+// rows and marches along z.  x-neighbours come from the neighbouring lanes
+// (shuffles; lanes 0 and 31 load the one cell beyond the warp), y-neighbours
+// from the thread's own column except the two rows just outside it, z
+// neighbours from the registers of the previous and next plane.  No shared
+// memory and no barriers; per plane a thread issues TY coalesced loads of
+// the next plane plus two rows of halo (L2 hits).
+template<typename T>
+__device__ __forceinline__ T shfl_down1(T v)
+{
+    return __shfl_down_sync(0xffffffffu, v, 1);
+}
+
+template<typename T>
+__device__ __forceinline__ T shfl_up1(T v)
+{
+    return __shfl_up_sync(0xffffffffu, v, 1);
+}
+
+template<typename CELL, int TY>
+__global__ void __launch_bounds__(128)
+jacobi7_zcol_kernel(View<const typename CELL::T> in, View<typename CELL::T> out, int periodic,
+                    typename CELL::T edge, int zchunk)
+{
+    typedef typename CELL::T T;
+    const int lane = threadIdx.x;
+    const int x = blockIdx.x * 32 + lane;
+    const int y0 = (blockIdx.y * blockDim.y + threadIdx.y) * TY;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, in.nz);
+    if (y0 >= in.ny) return;   // whole warp leaves together (y0 is warp-uniform)
+    const bool xin = x < in.nx;
+
+    T bel[TY], cur[TY], abv[TY];
+#pragma unroll
+    for (int j = 0; j < TY; ++j) {
+        bel[j] = load_any(in, x, y0 + j, z0 - 1, periodic, edge);
+        cur[j] = load_any(in, x, y0 + j, z0, periodic, edge);
+    }
+    for (int z = z0; z < z1; ++z) {
+#pragma unroll
+        for (int j = 0; j < TY; ++j) {
+            const int y = y0 + j;
+            abv[j] = (xin && y < in.ny && z + 1 < in.nz) ? in.at(x, y, z + 1) : load_any(in, x, y, z + 1, periodic, edge);
+        }
+        const T hn = load_any(in, x, y0 - 1, z, periodic, edge);
+        const T hs = load_any(in, x, y0 + TY, z, periodic, edge);
+#pragma unroll
+        for (int j = 0; j < TY; ++j) {
+            const int y = y0 + j;
+            T e = shfl_down1(cur[j]);
+            T w = shfl_up1(cur[j]);
+            if (lane == 31) e = load_any(in, x + 1, y, z, periodic, edge);
+            if (lane == 0) w = load_any(in, x - 1, y, z, periodic, edge);
+            const T n = (j == 0) ? hn : cur[j - 1];
+            const T s = (j == TY - 1) ? hs : cur[j + 1];
+            if (xin && y < in.ny) {
+                out.at(x, y, z) = CELL::apply(cur[j], n, s, e, w, abv[j], bel[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < TY; ++j) {
+            bel[j] = cur[j];
+            cur[j] = abv[j];
+        }
+    }
+}
+
 template<typename R>
 __global__ void __launch_bounds__(SBX * SBY)
 varcoef_zmarch_kernel(View<const R> u, View<const R> k, View<R> out, int periodic, R edgeU, R edgeK, int zchunk)
@@ -169,8 +237,53 @@ static dim3 zmarch_grid(const Grid& g, int *zchunk)
 
 long long fix_edge(const Grid& g);
 
+static const int ZCOL_TY = 4;   // rows per warp
+static const int ZCOL_WY = 4;   // warps per CTA
+
+static dim3 zcol_grid(const Grid& g, int *zchunk)
+{
+    const int bx = (g.desc.nx + 31) / 32;
+    const int by = (g.desc.ny + ZCOL_TY * ZCOL_WY - 1) / (ZCOL_TY * ZCOL_WY);
+    const long long xy = (long long)bx * by;
+    // about 16 resident CTAs of 128 threads per SM, several waves deep
+    int zsplit = (int)((152LL * 16 * 2 + xy - 1) / xy);
+    zsplit = max(1, min(zsplit, (g.desc.nz + 15) / 16));
+    *zchunk = (g.desc.nz + zsplit - 1) / zsplit;
+    zsplit = (g.desc.nz + *zchunk - 1) / *zchunk;
+    return dim3(bx, by, zsplit);
+}
+
+template<typename CELL>
+static void launch_zcol(Grid& g, View<const typename CELL::T> in, View<typename CELL::T> out, typename CELL::T edge)
+{
+    int zchunk = 1;
+    const dim3 grid = zcol_grid(g, &zchunk);
+    jacobi7_zcol_kernel<CELL, ZCOL_TY><<<grid, dim3(32, ZCOL_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge, zchunk);
+}
+
 void launch_jacobi7(Grid& g, int steps)
 {
+    if (g.variant == 0) {
+        for (int s = 0; s < steps; ++s) {
+            switch (g.desc.cell) {
+            case LGD_CELL_JACOBI7_F64:
+                launch_zcol<Jacobi7F64>(g, cmview<double>(g, 0, 0), mview<double>(g, 0, 1), g.desc.edge[0]);
+                break;
+            case LGD_CELL_JACOBI7_F32:
+                launch_zcol<Jacobi7F32>(g, cmview<float>(g, 0, 0), mview<float>(g, 0, 1), (float)g.desc.edge[0]);
+                break;
+            case LGD_CELL_JACOBI7_F64_FIX:
+                launch_zcol<Jacobi7Fix>(g, cmview<long long>(g, 0, 0), mview<long long>(g, 0, 1), fix_edge(g));
+                break;
+            default:
+                throw Error(LGD_ERR_UNSUPPORTED, "not a Jacobi cell");
+            }
+            check_launch("jacobi7");
+            ++g.launches;
+            g.cur = 1 - g.cur;
+        }
+        return;
+    }
     int zchunk = 1;
     dim3 grid = zmarch_grid(g, &zchunk);
     dim3 block(SBX, SBY);

@@ -86,7 +86,8 @@ struct Grid {
     size_t plane_elems;     // pitch_elems * ny
     int cur;                // index of the current buffer
     int time_block;         // temporal blocking depth (0 = default)
-    int fix_exp;            // fixed-point grids: value = k * 2^(fix_exp - 60)
+    int fix_exp;            // fixed-point grids: value = k * 2^(fix_exp - LGD_FIX_BITS)
+    int variant;            // kernel variant where a cell has several (0 = default)
     cudaStream_t stream;
     uint64_t launches;
     int device;

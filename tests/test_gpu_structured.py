@@ -95,7 +95,7 @@ def test_jacobi7_fixed_point_signed_values_and_edge():
     u0 = workloads.jacobi_initial(31, 17, 12, seed=9) * 6.0 - 3.0
     out = run_grid(lgd.CELL_JACOBI7_F64_FIX, [u0], 20, edge=(-2.5, 0, 0, 0))
     ref = oracle.jacobi7(u0, 20, edge=-2.5)
-    # the fixed-point grid adds at most 20 * 2^(2 - 61) ~ 3.5e-17; the FP64
+    # the fixed-point grid adds at most 20 * 2^(2 - 60) ~ 6.9e-17; the FP64
     # reference itself rounds each of its 7 operations per step (ulp(2.4) =
     # 4.4e-16), so the difference is dominated by the reference's own rounding
     assert np.max(np.abs(out - ref)) <= 20 * 7 * 4.5e-16
