@@ -575,7 +575,7 @@ int lgd_gpu_set_variant(lgd_handle *h, int variant)
 {
     return guard([&] {
         Grid& g = grid_of(h);
-        LGD_REQUIRE(variant == 0 || variant == 1, LGD_ERR_INVALID, "variant must be 0 or 1");
+        LGD_REQUIRE(variant >= 0 && variant <= 2, LGD_ERR_INVALID, "variant must be 0, 1 or 2");
         g.variant = variant;
     });
 }

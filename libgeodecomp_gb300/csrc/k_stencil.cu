@@ -139,6 +139,213 @@ jacobi7_zcol_kernel(View<const typename CELL::T> in, View<typename CELL::T> out,
     }
 }
 
+// Pair variant (default): like the register-column kernel, but every lane
+// owns two neighbouring x cells (one 16-byte load or store per row and
+// plane for 8-byte cells), so half of the x-neighbours are in the thread's
+// own registers; warps whose 64 x 4 footprint plus its one-cell rim lies
+// inside the grid take a path without any boundary test, and the z loop is
+// unrolled three times so the below / centre / above planes rotate through
+// register names instead of being copied.
+template<typename T>
+struct Pair {
+    T a, b;
+};
+
+template<typename T>
+__device__ __forceinline__ Pair<T> ld_pair(const T *p)
+{
+    Pair<T> r;
+    if (sizeof(T) == 8) {
+        const longlong2 v = *reinterpret_cast<const longlong2 *>(p);
+        r.a = *reinterpret_cast<const T *>(&v.x);
+        r.b = *reinterpret_cast<const T *>(&v.y);
+    } else {
+        const int2 v = *reinterpret_cast<const int2 *>(p);
+        r.a = *reinterpret_cast<const T *>(&v.x);
+        r.b = *reinterpret_cast<const T *>(&v.y);
+    }
+    return r;
+}
+
+template<typename T>
+__device__ __forceinline__ void st_pair(T *p, T a, T b)
+{
+    if (sizeof(T) == 8) {
+        longlong2 v;
+        v.x = *reinterpret_cast<const long long *>(&a);
+        v.y = *reinterpret_cast<const long long *>(&b);
+        *reinterpret_cast<longlong2 *>(p) = v;
+    } else {
+        int2 v;
+        v.x = *reinterpret_cast<const int *>(&a);
+        v.y = *reinterpret_cast<const int *>(&b);
+        *reinterpret_cast<int2 *>(p) = v;
+    }
+}
+
+// Everything a warp of the pair kernel needs to address its footprint: the
+// warp owns x in [x0 - 2 lane, + 64), rows [y0, y0 + TY) and all of them
+// exist.  Rows and planes outside the grid are either wrapped (periodic
+// axis) or replaced by the edge value; those decisions are uniform across
+// the warp.  Only lanes 0 and 31 look one cell beyond the warp in x.
+template<typename T, int TY>
+struct PairFrame {
+    const T *in;
+    T *out;
+    long pitch;
+    long plane;
+    int nx, ny, nz;
+    int periodic;
+    int x0, y0, lane;
+    T edge;
+
+    // row y of plane z of the input at column x0, or null for "edge"
+    __device__ __forceinline__ const T *row(int y, int z) const
+    {
+        if (y < 0 || y >= ny) {
+            if (!(periodic & 2)) return nullptr;
+            y = (y < 0) ? y + ny : y - ny;
+        }
+        if (z < 0 || z >= nz) {
+            if (!(periodic & 4)) return nullptr;
+            z = (z < 0) ? z + nz : z - nz;
+        }
+        return in + (long)z * plane + (long)y * pitch + x0;
+    }
+
+    __device__ __forceinline__ Pair<T> pair_at(const T *r) const
+    {
+        if (r) return ld_pair(r);
+        Pair<T> e;
+        e.a = edge;
+        e.b = edge;
+        return e;
+    }
+
+    __device__ __forceinline__ void load_plane(int z, Pair<T> (&P)[TY]) const
+    {
+        const T *r = row(y0, z);   // the TY rows are all inside in y
+#pragma unroll
+        for (int j = 0; j < TY; ++j) P[j] = pair_at(r ? r + j * pitch : nullptr);
+    }
+
+    // cell x0 - 1 (lane 0) or x0 + 2 (lane 31) of row r (r points at x0)
+    __device__ __forceinline__ T west(const T *r) const
+    {
+        if (x0 >= 1) return r[-1];
+        return (periodic & 1) ? r[nx - 1 - x0] : edge;
+    }
+
+    __device__ __forceinline__ T east(const T *r) const
+    {
+        if (x0 + 2 < nx) return r[2];
+        return (periodic & 1) ? r[-x0] : edge;
+    }
+};
+
+// Plane z: B / C / A hold planes z - 1, z, z + 1; N receives plane z + 2
+// when load_next is set.
+template<typename CELL, int TY>
+__device__ __forceinline__ void pair_plane(const PairFrame<typename CELL::T, TY>& f, int z, bool load_next,
+                                           const Pair<typename CELL::T> (&B)[TY], const Pair<typename CELL::T> (&C)[TY],
+                                           const Pair<typename CELL::T> (&A)[TY], Pair<typename CELL::T> (&N)[TY])
+{
+    typedef typename CELL::T T;
+    if (load_next) f.load_plane(z + 2, N);
+    const T *r = f.in + (long)z * f.plane + (long)f.y0 * f.pitch + f.x0;
+    const Pair<T> hn = f.pair_at(f.row(f.y0 - 1, z));
+    const Pair<T> hs = f.pair_at(f.row(f.y0 + TY, z));
+    T *o = f.out + (long)z * f.plane + (long)f.y0 * f.pitch + f.x0;
+#pragma unroll
+    for (int j = 0; j < TY; ++j) {
+        T w0 = shfl_up1(C[j].b);
+        T e1 = shfl_down1(C[j].a);
+        if (f.lane == 0) w0 = f.west(r + j * f.pitch);
+        if (f.lane == 31) e1 = f.east(r + j * f.pitch);
+        const Pair<T> n = (j == 0) ? hn : C[j - 1];
+        const Pair<T> s = (j == TY - 1) ? hs : C[j + 1];
+        const T o0 = CELL::apply(C[j].a, n.a, s.a, C[j].b, w0, A[j].a, B[j].a);
+        const T o1 = CELL::apply(C[j].b, n.b, s.b, e1, C[j].a, A[j].b, B[j].b);
+        st_pair(o + j * f.pitch, o0, o1);
+    }
+}
+
+template<typename CELL, int TY>
+__global__ void __launch_bounds__(64)
+jacobi7_pair_kernel(View<const typename CELL::T> in, View<typename CELL::T> out, int periodic,
+                    typename CELL::T edge, int zchunk)
+{
+    typedef typename CELL::T T;
+    const int lane = threadIdx.x;
+    const int xb = blockIdx.x * 64;
+    const int x0 = xb + 2 * lane;
+    const int y0 = (blockIdx.y * blockDim.y + threadIdx.y) * TY;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, in.nz);
+    if (y0 >= in.ny) return;   // warp-uniform
+
+    if (xb + 64 <= in.nx && y0 + TY <= in.ny) {
+        // full warp footprint: vector path
+        PairFrame<T, TY> f;
+        f.in = in.p;
+        f.out = out.p;
+        f.pitch = in.pitch;
+        f.plane = in.pitch * in.ny;
+        f.nx = in.nx;
+        f.ny = in.ny;
+        f.nz = in.nz;
+        f.periodic = periodic;
+        f.x0 = x0;
+        f.y0 = y0;
+        f.lane = lane;
+        f.edge = edge;
+        Pair<T> P0[TY], P1[TY], P2[TY], P3[TY];
+        f.load_plane(z0 - 1, P0);
+        f.load_plane(z0, P1);
+        f.load_plane(z0 + 1, P2);
+        // four register sets rotate: plane z uses (below, centre, above) and
+        // fills the fourth with plane z + 2, which plane z + 1 needs
+        for (int z = z0; z < z1; z += 4) {
+            pair_plane<CELL, TY>(f, z, z + 1 < z1, P0, P1, P2, P3);
+            if (z + 1 >= z1) break;
+            pair_plane<CELL, TY>(f, z + 1, z + 2 < z1, P1, P2, P3, P0);
+            if (z + 2 >= z1) break;
+            pair_plane<CELL, TY>(f, z + 2, z + 3 < z1, P2, P3, P0, P1);
+            if (z + 3 >= z1) break;
+            pair_plane<CELL, TY>(f, z + 3, z + 4 < z1, P3, P0, P1, P2);
+        }
+        return;
+    }
+
+    // partial footprint (grid edge in x or y): per-cell loads
+    const bool xin0 = x0 < in.nx;
+    const bool xin1 = x0 + 1 < in.nx;
+    for (int z = z0; z < z1; ++z) {
+#pragma unroll
+        for (int j = 0; j < TY; ++j) {
+            const int y = y0 + j;
+            const T c0 = load_any(in, x0, y, z, periodic, edge);
+            const T c1 = load_any(in, x0 + 1, y, z, periodic, edge);
+            T w0 = shfl_up1(c1);
+            T e1 = shfl_down1(c0);
+            if (lane == 0) w0 = load_any(in, x0 - 1, y, z, periodic, edge);
+            if (lane == 31) e1 = load_any(in, x0 + 2, y, z, periodic, edge);
+            if (xin0 && y < in.ny) {
+                out.at(x0, y, z) = CELL::apply(c0, load_any(in, x0, y - 1, z, periodic, edge),
+                                               load_any(in, x0, y + 1, z, periodic, edge), c1, w0,
+                                               load_any(in, x0, y, z + 1, periodic, edge),
+                                               load_any(in, x0, y, z - 1, periodic, edge));
+            }
+            if (xin1 && y < in.ny) {
+                out.at(x0 + 1, y, z) = CELL::apply(c1, load_any(in, x0 + 1, y - 1, z, periodic, edge),
+                                                   load_any(in, x0 + 1, y + 1, z, periodic, edge), e1, c0,
+                                                   load_any(in, x0 + 1, y, z + 1, periodic, edge),
+                                                   load_any(in, x0 + 1, y, z - 1, periodic, edge));
+            }
+        }
+    }
+}
+
 template<typename R>
 __global__ void __launch_bounds__(SBX * SBY)
 varcoef_zmarch_kernel(View<const R> u, View<const R> k, View<R> out, int periodic, R edgeU, R edgeK, int zchunk)
@@ -253,17 +460,40 @@ static dim3 zcol_grid(const Grid& g, int *zchunk)
     return dim3(bx, by, zsplit);
 }
 
+static const int PAIR_TY = 4;   // rows per warp
+static const int PAIR_WY = 2;   // warps per CTA
+
+static dim3 pair_grid(const Grid& g, int *zchunk)
+{
+    const int bx = (g.desc.nx + 63) / 64;
+    const int by = (g.desc.ny + PAIR_TY * PAIR_WY - 1) / (PAIR_TY * PAIR_WY);
+    const long long xy = (long long)bx * by;
+    // about 24 resident CTAs of 64 threads per SM, two waves
+    int zsplit = (int)((152LL * 24 * 2 + xy - 1) / xy);
+    zsplit = max(1, min(zsplit, (g.desc.nz + 15) / 16));
+    *zchunk = (g.desc.nz + zsplit - 1) / zsplit;
+    zsplit = (g.desc.nz + *zchunk - 1) / *zchunk;
+    return dim3(bx, by, zsplit);
+}
+
 template<typename CELL>
 static void launch_zcol(Grid& g, View<const typename CELL::T> in, View<typename CELL::T> out, typename CELL::T edge)
 {
     int zchunk = 1;
-    const dim3 grid = zcol_grid(g, &zchunk);
-    jacobi7_zcol_kernel<CELL, ZCOL_TY><<<grid, dim3(32, ZCOL_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge, zchunk);
+    if (g.variant == 2) {
+        const dim3 grid = zcol_grid(g, &zchunk);
+        jacobi7_zcol_kernel<CELL, ZCOL_TY><<<grid, dim3(32, ZCOL_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge,
+                                                                                    zchunk);
+    } else {
+        const dim3 grid = pair_grid(g, &zchunk);
+        jacobi7_pair_kernel<CELL, PAIR_TY><<<grid, dim3(32, PAIR_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge,
+                                                                                    zchunk);
+    }
 }
 
 void launch_jacobi7(Grid& g, int steps)
 {
-    if (g.variant == 0) {
+    if (g.variant != 1) {
         for (int s = 0; s < steps; ++s) {
             switch (g.desc.cell) {
             case LGD_CELL_JACOBI7_F64:

@@ -295,3 +295,42 @@ def test_varcoef_f32_error_against_fp64():
     ref = oracle.varcoef(u0, k, 64)
     rel_l2 = np.linalg.norm(out.astype(np.float64) - ref) / np.linalg.norm(ref)
     assert rel_l2 < 1e-6, rel_l2
+
+
+# ------------------------------------------ kernel variants and fast paths
+def _set_variant(g, v):
+    fn = lgd.lib().lgd_gpu_set_variant
+    fn.argtypes = [lgd.ctypes.c_void_p, lgd.ctypes.c_int]
+    lgd.check(fn(g._h, v))
+
+
+@pytest.mark.parametrize("shape,periodic", [((9, 20, 128), 0), ((9, 20, 128), 7), ((70, 16, 64), 0),
+                                            ((70, 16, 64), 7), ((3, 4, 64), 7), ((1, 8, 192), 0),
+                                            ((33, 13, 130), 7), ((17, 7, 96), 0)])
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_jacobi7_variants_bit_exact_on_wide_grids(shape, periodic, variant):
+    """Shapes whose x extent fills whole 64-wide warps take the vector path
+    of the default kernel; all variants must equal the oracle bit for bit."""
+    u0 = workloads.jacobi_initial(shape[2], shape[1], shape[0], seed=13)
+    with lgd.Grid(lgd.CELL_JACOBI7_F64, shape, periodic=periodic, edge=(0.5, 0, 0, 0)) as g:
+        _set_variant(g, variant)
+        g.upload(0, u0)
+        g.step(5)
+        out = g.download(0)
+    np.testing.assert_array_equal(out, oracle.jacobi7(u0, 5, torus=periodic == 7, edge=0.5))
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_jacobi7_fixed_point_variants_identical(variant):
+    u0 = workloads.jacobi_initial(128, 24, 40, seed=14)
+    with lgd.Grid(lgd.CELL_JACOBI7_F64_FIX, u0.shape) as g:
+        _set_variant(g, variant)
+        g.upload(0, u0)
+        g.step(6)
+        out = g.download(0)
+    with lgd.Grid(lgd.CELL_JACOBI7_F64_FIX, u0.shape) as g:
+        _set_variant(g, 1)
+        g.upload(0, u0)
+        g.step(6)
+        ref = g.download(0)
+    np.testing.assert_array_equal(out, ref)
