@@ -267,7 +267,65 @@ class SellWorkload:
         self.g.close()
 
 
+class LbmWorkload:
+    """512 D3Q19 lid-driven cavities, edges uniform in {32..192}, omega
+    uniform in [1.0, 1.9), lid 0.05, FP32; one persistent launch per step,
+    launch shape from the library's pattern-search tuner."""
+    run_steps = 500
+    bytes_per_unit = 152     # 19 FP32 reads + 19 FP32 writes per cell
+
+    def __init__(self):
+        from libgeodecomp_gb300 import lgd, workloads
+        self.lgd = lgd
+        self.name = "lbm_d3q19_ensemble_512"
+        self.metric = "D3Q19 ensemble GLUPS (one persistent launch per step)"
+        self.unit = "GLUPS"
+        self.dtype = "f32"
+        edges, omegas = workloads.lbm_ensemble(512, seed=42)
+        self.e = lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=4)
+        self.units, self.items = self.e.info()
+        (ty, th, ct), best = self.e.tune(trial_steps=2)
+        self.e.reset()
+        self.config = {"workload": self.name, "instances": 512, "edges": "uniform {32..192}",
+                       "omega": "uniform [1.0, 1.9)", "lid": 0.05, "cells": self.units, "work_items": self.items,
+                       "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct},
+                       "l2": "166 GB of populations, far larger than L2"}
+
+    def stream(self):
+        return self.e.stream()
+
+    def step(self, n=1):
+        self.e.step(n)
+
+    def sync(self):
+        self.e.synchronize()
+
+    def launches(self):
+        return self.e.launch_count()
+
+    def host_buffers(self, torch):
+        return None, None
+
+    def e2e_run(self, hin, hout):
+        raise NotImplementedError
+
+    def looped_ms(self, torch, steps):
+        st = torch.cuda.ExternalStream(self.e.stream())
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        self.e.step_looped(steps)
+        b.record(st)
+        b.synchronize()
+        return a.elapsed_time(b) / steps
+
+    def close(self):
+        self.e.close()
+
+
 def make_workload(name, size=512):
+    if name == "lbm_d3q19_ensemble_512":
+        return LbmWorkload()
     if name == "jacobi7_f64_512":
         return JacobiWorkload(ieee=False, edge=size)
     if name == "jacobi7_f64_ieee_512":
@@ -279,7 +337,7 @@ def make_workload(name, size=512):
     raise ValueError(name)
 
 
-WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "gol_u8_8192", "sell_f64_4m"]
+WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "gol_u8_8192", "sell_f64_4m", "lbm_d3q19_ensemble_512"]
 
 
 # ------------------------------------------------------------------ helpers
@@ -351,7 +409,7 @@ def run_gpu(args, world, rank, local, dist):
                 "traffic": traffic}
 
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and args.workload != "lbm_d3q19_ensemble_512":
         hin, hout = w.host_buffers(torch)
         w.e2e_run(hin, hout)     # warm-up
         runs = max(1, args.e2e_runs)
@@ -382,6 +440,12 @@ def run_gpu(args, world, rank, local, dist):
             "note": "LGD_CELL_JACOBI7_F64: bit-identical to the reference; bound by the GPU's FP64 rate"}
         wi.close()
     else:
+        if args.workload == "lbm_d3q19_ensemble_512":
+            # the same steps with one launch per instance (512 launches per step)
+            lms = w.looped_ms(torch, max(2, args.steps // 4))
+            extra["looped_single_grid_launches"] = {"ms_per_step": round(lms, 3),
+                                                    "glups": round(w.units / (lms * 1e-3) / 1e9, 2)}
+            extra["e2e_note"] = "no host round trip: the 166 GB ensemble lives on the device"
         w.close()
     if args.workload == "sell_f64_4m":
         extra["s_per_step"] = round(ms_per_step * 1e-3, 7)

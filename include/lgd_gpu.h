@@ -118,6 +118,12 @@ int lgd_gpu_destroy(lgd_handle *h);
 int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_t bytes);
 int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t bytes);
 
+/* The same copies from / to dense DEVICE memory of another owner (device
+ * pipelines: the surrogate, frameworks holding their own buffers);
+ * synchronise the handle's stream.  Not for LGD_CELL_JACOBI7_F64_FIX. */
+int lgd_gpu_upload_device(lgd_handle *h, int member, int which, const void *dev, size_t bytes);
+int lgd_gpu_download_device(lgd_handle *h, int member, int which, void *dev, size_t bytes);
+
 /* Streak-wise copies for plugins that need part of the grid (reference:
  * GridBase::saveRegion / loadRegion, storage/gridbase.h; the libflatarray
  * streak functors save_functor.hpp / load_functor.hpp).  streaks holds

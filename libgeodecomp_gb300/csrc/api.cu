@@ -392,6 +392,28 @@ int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t by
     });
 }
 
+static void device_copy(lgd_handle *h, int member, int which, void *dev, size_t bytes, bool to_grid)
+{
+    Grid& g = grid_of(h);
+    check_member(g, member, which);
+    LGD_REQUIRE(g.desc.cell != LGD_CELL_JACOBI7_F64_FIX, LGD_ERR_UNSUPPORTED,
+                "device copies of the fixed-point grid are not supported");
+    const size_t n = cells_of(g);
+    const size_t elem = (size_t)g.m[member].elem;
+    LGD_REQUIRE(dev != nullptr, LGD_ERR_INVALID, "null device buffer");
+    LGD_REQUIRE(bytes == n * elem, LGD_ERR_INVALID, "byte count does not match the grid");
+    const size_t rows = (size_t)g.desc.ny * g.desc.nz;
+    const size_t row_bytes = (size_t)g.desc.nx * elem;
+    if (to_grid) {
+        LGD_CHECK_CUDA(cudaMemcpy2DAsync(member_buf(g, member, which), g.pitch_bytes[member], dev, row_bytes, row_bytes,
+                                         rows, cudaMemcpyDeviceToDevice, g.stream));
+    } else {
+        LGD_CHECK_CUDA(cudaMemcpy2DAsync(dev, row_bytes, member_buf(g, member, which), g.pitch_bytes[member], row_bytes,
+                                         rows, cudaMemcpyDeviceToDevice, g.stream));
+    }
+    LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+}
+
 static void region_copy(lgd_handle *h, int member, const int *streaks, int n_streaks, void *host,
                         size_t bytes, bool to_grid)
 {
@@ -415,6 +437,16 @@ static void region_copy(lgd_handle *h, int member, const int *streaks, int n_str
     }
     LGD_CHECK_CUDA(cudaFreeAsync(d, g.stream));
     LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+}
+
+int lgd_gpu_upload_device(lgd_handle *h, int member, int which, const void *dev, size_t bytes)
+{
+    return guard([&] { device_copy(h, member, which, const_cast<void *>(dev), bytes, true); });
+}
+
+int lgd_gpu_download_device(lgd_handle *h, int member, int which, void *dev, size_t bytes)
+{
+    return guard([&] { device_copy(h, member, which, dev, bytes, false); });
 }
 
 int lgd_gpu_save_region(lgd_handle *h, int member, const int *streaks, int n_streaks, void *host, size_t bytes)
