@@ -607,7 +607,7 @@ int lgd_gpu_set_variant(lgd_handle *h, int variant)
 {
     return guard([&] {
         Grid& g = grid_of(h);
-        LGD_REQUIRE(variant >= 0 && variant <= 2, LGD_ERR_INVALID, "variant must be 0, 1 or 2");
+        LGD_REQUIRE(variant >= 0 && variant <= 4, LGD_ERR_INVALID, "variant must lie in [0, 4]");
         g.variant = variant;
     });
 }

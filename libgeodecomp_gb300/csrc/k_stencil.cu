@@ -463,10 +463,10 @@ static dim3 zcol_grid(const Grid& g, int *zchunk)
 static const int PAIR_TY = 4;   // rows per warp
 static const int PAIR_WY = 2;   // warps per CTA
 
-static dim3 pair_grid(const Grid& g, int *zchunk)
+static dim3 pair_grid(const Grid& g, int ty, int *zchunk)
 {
     const int bx = (g.desc.nx + 63) / 64;
-    const int by = (g.desc.ny + PAIR_TY * PAIR_WY - 1) / (PAIR_TY * PAIR_WY);
+    const int by = (g.desc.ny + ty * PAIR_WY - 1) / (ty * PAIR_WY);
     const long long xy = (long long)bx * by;
     // about 24 resident CTAs of 64 threads per SM, two waves
     int zsplit = (int)((152LL * 24 * 2 + xy - 1) / xy);
@@ -484,8 +484,14 @@ static void launch_zcol(Grid& g, View<const typename CELL::T> in, View<typename 
         const dim3 grid = zcol_grid(g, &zchunk);
         jacobi7_zcol_kernel<CELL, ZCOL_TY><<<grid, dim3(32, ZCOL_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge,
                                                                                     zchunk);
+    } else if (g.variant == 3) {
+        const dim3 grid = pair_grid(g, 8, &zchunk);
+        jacobi7_pair_kernel<CELL, 8><<<grid, dim3(32, PAIR_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge, zchunk);
+    } else if (g.variant == 4) {
+        const dim3 grid = pair_grid(g, 2, &zchunk);
+        jacobi7_pair_kernel<CELL, 2><<<grid, dim3(32, PAIR_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge, zchunk);
     } else {
-        const dim3 grid = pair_grid(g, &zchunk);
+        const dim3 grid = pair_grid(g, PAIR_TY, &zchunk);
         jacobi7_pair_kernel<CELL, PAIR_TY><<<grid, dim3(32, PAIR_WY), 0, g.stream>>>(in, out, g.desc.periodic, edge,
                                                                                     zchunk);
     }
