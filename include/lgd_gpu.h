@@ -163,9 +163,11 @@ int lgd_gpu_fill_bernoulli(lgd_handle *h, int member, int which, uint64_t seed, 
 int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
 
 /* Kernel variant for the Jacobi cells (results are identical): 0 (default)
- * two cells per lane, 4 rows per warp, marching in z with register
- * rotation and warp shuffles; 1 shared-memory plane tiles; 2 one cell per
- * lane; 3 / 4 as 0 with 8 / 2 rows per warp.  For tuning and comparison. */
+ * TMA-staged shared-memory planes on cube grids with a zero edge cell,
+ * otherwise variant 5; 1 shared-memory plane tiles loaded by the threads;
+ * 2 one cell per lane in registers; 3 / 4 / 5 two cells per lane, 8 / 2 / 4
+ * rows per warp, marching in z with register rotation and warp shuffles.
+ * For tuning and comparison. */
 int lgd_gpu_set_variant(lgd_handle *h, int variant);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or

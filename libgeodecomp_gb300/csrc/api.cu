@@ -147,6 +147,18 @@ static void raise_fix_exp(Grid& g, int e)
 }
 
 // --------------------------------------------------------------- helpers
+// Reads (and clears) the device error word that kernels with bounded waits
+// set when a wait gave up; call after the stream is synchronised.
+static void check_device_error(Grid& g)
+{
+    int e = 0;
+    LGD_CHECK_CUDA(cudaMemcpy(&e, g.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        LGD_CHECK_CUDA(cudaMemset(g.d_err, 0, sizeof(int)));
+        throw Error(LGD_ERR_TIMEOUT, "a device-side wait gave up; the last step's results are incomplete");
+    }
+}
+
 static Grid& grid_of(lgd_handle *h)
 {
     LGD_REQUIRE(h != nullptr, LGD_ERR_INVALID, "null handle");
@@ -266,6 +278,8 @@ int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
         LGD_CHECK_CUDA(cudaGetDevice(&g.device));
         try {
             LGD_CHECK_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+            LGD_CHECK_CUDA(cudaMalloc(&g.d_err, sizeof(int)));
+            LGD_CHECK_CUDA(cudaMemsetAsync(g.d_err, 0, sizeof(int), g.stream));
             for (int m = 0; m < ci.n_members; ++m) {
                 g.m[m].elem = ci.elem[m];
                 g.m[m].is_static = ci.is_static[m];
@@ -310,6 +324,7 @@ int lgd_gpu_destroy(lgd_handle *h)
         if (g.d_streaks) cudaFree(g.d_streaks);
         if (g.d_streak_prefix) cudaFree(g.d_streak_prefix);
         if (g.d_partials) cudaFree(g.d_partials);
+        if (g.d_err) cudaFree(g.d_err);
         cudaStreamDestroy(g.stream);
         delete h;
     });
@@ -383,12 +398,14 @@ int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t by
             LGD_CHECK_CUDA(cudaMemcpyAsync(host, tmp, n * 8, cudaMemcpyDeviceToHost, g.stream));
             LGD_CHECK_CUDA(cudaFreeAsync(tmp, g.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            check_device_error(g);
             return;
         }
         LGD_CHECK_CUDA(cudaMemcpy2DAsync(host, (size_t)g.desc.nx * helem, member_buf(g, member, which),
                                          g.pitch_bytes[member], (size_t)g.desc.nx * helem, rows,
                                          cudaMemcpyDeviceToHost, g.stream));
         LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+        check_device_error(g);
     });
 }
 
@@ -571,6 +588,7 @@ int lgd_gpu_synchronize(lgd_handle *h)
     return guard([&] {
         Grid& g = grid_of(h);
         LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+        check_device_error(g);
     });
 }
 
@@ -607,7 +625,7 @@ int lgd_gpu_set_variant(lgd_handle *h, int variant)
 {
     return guard([&] {
         Grid& g = grid_of(h);
-        LGD_REQUIRE(variant >= 0 && variant <= 4, LGD_ERR_INVALID, "variant must lie in [0, 4]");
+        LGD_REQUIRE(variant >= 0 && variant <= 5, LGD_ERR_INVALID, "variant must lie in [0, 5]");
         g.variant = variant;
     });
 }

@@ -499,6 +499,10 @@ static void launch_zcol(Grid& g, View<const typename CELL::T> in, View<typename 
 
 void launch_jacobi7(Grid& g, int steps)
 {
+    if (g.variant == 0 && tma_applicable(g)) {
+        for (int s = 0; s < steps; ++s) launch_jacobi7_tma(g);
+        return;
+    }
     if (g.variant != 1) {
         for (int s = 0; s < steps; ++s) {
             switch (g.desc.cell) {

@@ -97,7 +97,16 @@ struct Grid {
     int streak_capacity;
     double *d_partials;
     int partial_capacity;
+    // TMA kernel: one tensor map (a 128-byte CUtensorMap) per buffer, the
+    // buffer it was built for, and the device error word of bounded waits
+    alignas(64) unsigned char tmap[2][128];
+    bool tmap_ready[2];
+    void *tmap_base[2];
+    int *d_err;
 };
+
+bool tma_applicable(const Grid& g);
+void launch_jacobi7_tma(Grid& g);
 
 // kernels, one entry per cell family (implemented in k_*.cu)
 void launch_jacobi7(Grid& g, int steps);

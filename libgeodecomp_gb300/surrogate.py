@@ -327,7 +327,8 @@ def run_surrogate_with_judge(params, u0, kappa, steps: int, tol: float = 1e-4, c
             err = rel_l2(u, check)
             stats["judge_errors"].append(err)
             stats["segments"] += 1
-            if err > tol:
+            if not (err <= tol):     # a non-finite error fails the judge too
+
                 stats["fallbacks"] += 1
                 u.copy_(seg_start)
                 plain.run(u, seg_steps)

@@ -334,3 +334,32 @@ def test_jacobi7_fixed_point_variants_identical(variant):
         g.step(6)
         ref = g.download(0)
     np.testing.assert_array_equal(out, ref)
+
+
+TMA_SHAPES = [(9, 20, 128), (70, 16, 64), (1, 8, 192), (33, 13, 130), (17, 7, 96), (2, 1, 37), (5, 40, 70),
+              (3, 17, 1), (40, 33, 65)]
+
+
+@pytest.mark.parametrize("shape", TMA_SHAPES)
+def test_jacobi7_tma_kernel_bit_exact_fp64(shape):
+    """Cube grids with a zero edge cell run the TMA-staged kernel (variant 0):
+    ragged tiles in x and y, z chunks of one or a few planes."""
+    u0 = workloads.jacobi_initial(shape[2], shape[1], shape[0], seed=17)
+    out = run_grid(lgd.CELL_JACOBI7_F64, [u0], 7)
+    np.testing.assert_array_equal(out, oracle.jacobi7(u0, 7))
+
+
+@pytest.mark.parametrize("shape", TMA_SHAPES)
+@pytest.mark.parametrize("cell", [lgd.CELL_JACOBI7_F64_FIX, lgd.CELL_JACOBI7_F32])
+def test_jacobi7_tma_kernel_equals_register_kernel(shape, cell):
+    u0 = workloads.jacobi_initial(shape[2], shape[1], shape[0], seed=18)
+    if cell == lgd.CELL_JACOBI7_F32:
+        u0 = u0.astype(np.float32)
+    res = []
+    for variant in (0, 5):
+        with lgd.Grid(cell, shape) as g:
+            _set_variant(g, variant)
+            g.upload(0, u0)
+            g.step(7)
+            res.append(g.download(0))
+    np.testing.assert_array_equal(res[0], res[1])
