@@ -274,18 +274,23 @@ class LbmWorkload:
     run_steps = 500
     bytes_per_unit = 152     # 19 FP32 reads + 19 FP32 writes per cell
 
-    def __init__(self):
+    def __init__(self, instances=512, edge_max=192, tune=True):
         from libgeodecomp_gb300 import lgd, workloads
         self.lgd = lgd
         self.name = "lbm_d3q19_ensemble_512"
         self.metric = "D3Q19 ensemble GLUPS (one persistent launch per step)"
         self.unit = "GLUPS"
         self.dtype = "f32"
-        edges, omegas = workloads.lbm_ensemble(512, seed=42)
+        # the configuration is 512 instances with edges up to 192; smaller
+        # ensembles serve profiling captures
+        edges, omegas = workloads.lbm_ensemble(instances, seed=42, edge_max=edge_max)
         self.e = lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=4)
         self.units, self.items = self.e.info()
-        (ty, th, ct), best = self.e.tune(trial_steps=2)
-        self.e.reset()
+        if tune:
+            (ty, th, ct), best = self.e.tune(trial_steps=2)
+            self.e.reset()
+        else:
+            ty, th, ct = self.e.config()
         self.config = {"workload": self.name, "instances": 512, "edges": "uniform {32..192}",
                        "omega": "uniform [1.0, 1.9)", "lid": 0.05, "cells": self.units, "work_items": self.items,
                        "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct},
@@ -323,9 +328,9 @@ class LbmWorkload:
         self.e.close()
 
 
-def make_workload(name, size=512):
+def make_workload(name, size=512, lbm_instances=512, lbm_edge_max=192, lbm_tune=True):
     if name == "lbm_d3q19_ensemble_512":
-        return LbmWorkload()
+        return LbmWorkload(instances=lbm_instances, edge_max=lbm_edge_max, tune=lbm_tune)
     if name == "jacobi7_f64_512":
         return JacobiWorkload(ieee=False, edge=size)
     if name == "jacobi7_f64_ieee_512":
@@ -381,7 +386,7 @@ def time_steps(torch, w, steps):
 def run_gpu(args, world, rank, local, dist):
     import torch
     torch.cuda.set_device(local)
-    w = make_workload(args.workload, args.size)
+    w = make_workload(args.workload, args.size, args.lbm_instances, args.lbm_edge_max, not args.lbm_no_tune)
     for _ in range(args.warmup):
         w.step(1)
     w.sync()
@@ -533,6 +538,60 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_surrogate(args):
+    """Learned surrogate for variable-coefficient diffusion on 256^3 FP32 to
+    t = 4096 steps: train on plain-stencil trajectories (GPU, the library's
+    own forward / backward / Adam kernels), then time surrogate plus judge
+    against the plain FP32 stencil, both measured against the FP64 stencil."""
+    import torch
+    from libgeodecomp_gb300 import surrogate as S
+    from libgeodecomp_gb300 import workloads
+    n = args.surrogate_size
+    steps = args.surrogate_steps
+    t0 = time.perf_counter()
+    states, kappa_tr = S.make_trajectories(count=args.trajectories, n=32, calls=4, length=16.0, seed=7)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    params, hist = S.train(states, kappa_tr, channels=24, iters=args.train_iters, batch=8, lr=1e-3, seed=1)
+    t_train = time.perf_counter() - t0
+    err_net, err_id = S.one_call_errors(params, states[-64:], kappa_tr[-64:], channels=24)
+    del states, kappa_tr
+
+    u0_np, k_np = workloads.varcoef_fields(n, seed=42, length=16.0)
+    u0 = torch.tensor(u0_np, dtype=torch.float32, device="cuda").contiguous()
+    kap = torch.tensor(k_np, dtype=torch.float32, device="cuda").contiguous()
+    # FP64 reference with the FP64 stencil (bit-identical to the reference's
+    # simulator at small sizes, see tests)
+    ref = S.PlainStencil(n, precision=8)
+    try:
+        u64 = torch.tensor(u0_np, dtype=torch.float64, device="cuda").contiguous()
+        ref.set_kappa(torch.tensor(k_np, dtype=torch.float64, device="cuda").contiguous())
+        ref.run(u64, steps)
+    finally:
+        ref.close()
+    S.run_plain(u0, kap, 16)                         # warm-up
+    u_plain, t_plain = S.run_plain(u0, kap, steps)
+    u_sur, t_sur, stats = S.run_surrogate_with_judge(params, u0, kap, steps, tol=args.judge_tol)
+    line = {
+        "metric": "surrogate vs plain time at rel-L2<=1e-3", "value": round(t_plain / t_sur, 4),
+        "unit": "x (plain FP32 stencil time / surrogate-plus-judge time)", "higher_is_better": True,
+        "n_gpus": 1, "steps": steps, "warmup": 1, "dtype": "bf16 net (fp32 accumulate), fp32 plain stencil",
+        "data": "synthetic (seeded Gaussian random fields)", "vs_baseline": None, "scaling": "weak",
+        "config": {"workload": "surrogate_varcoef_%d" % n, "grid": [n, n, n], "t_final": steps,
+                   "kappa": "GRF length 16 mapped to [0.02, 0.15]", "net": "4 x conv3^3, 24 ch, GELU, residual",
+                   "steps_per_call": S.STEPS_PER_CALL, "judge_every_calls": S.CALLS_PER_JUDGE,
+                   "judge_tol": args.judge_tol, "trajectories": args.trajectories, "train_iters": args.train_iters},
+        "plain_fp32_s": round(t_plain, 4), "surrogate_judge_s": round(t_sur, 4),
+        "rel_l2_vs_fp64": {"plain_fp32": S.rel_l2(u_plain, u64), "surrogate_judge": S.rel_l2(u_sur, u64)},
+        "judge": {"segments": stats["segments"], "fallbacks": stats["fallbacks"],
+                  "max_error": max(stats["judge_errors"]) if stats["judge_errors"] else None},
+        "training": {"data_s": round(t_data, 2), "train_s": round(t_train, 2), "loss_first": hist[0],
+                     "loss_last": float(np.mean(hist[-20:])),
+                     "one_call_rel_l2": {"net": float(err_net), "no_learning_baseline": float(err_id)}},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -546,9 +605,21 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ieee", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lbm-instances", type=int, default=512, help="ensemble size (smaller for profiling captures)")
+    ap.add_argument("--lbm-edge-max", type=int, default=192)
+    ap.add_argument("--lbm-no-tune", action="store_true", help="keep the default launch shape (profiling captures)")
+    ap.add_argument("--surrogate", action="store_true", help="run the learned-surrogate time-to-solution benchmark")
+    ap.add_argument("--surrogate-size", type=int, default=256)
+    ap.add_argument("--surrogate-steps", type=int, default=4096)
+    ap.add_argument("--trajectories", type=int, default=2000)
+    ap.add_argument("--train-iters", type=int, default=1500)
+    ap.add_argument("--judge-tol", type=float, default=1e-4)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.surrogate:
+        run_surrogate(args)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
