@@ -550,8 +550,148 @@ void launch_jacobi7(Grid& g, int steps)
     }
 }
 
+// Variable-coefficient diffusion with the pair kernel's scheme (two x cells
+// per lane, TY rows per warp, z rotation through four register sets,
+// warp-uniform wrap / edge decisions), carrying u and k.  Traffic: u read,
+// k read, u written: 12 B per cell for FP32.
+template<typename R, int TY>
+__device__ __forceinline__ void varcoef_pair_plane(const PairFrame<R, TY>& fu, const PairFrame<R, TY>& fk, int z,
+                                                   bool load_next, const Pair<R> (&UB)[TY], const Pair<R> (&UC)[TY],
+                                                   const Pair<R> (&UA)[TY], Pair<R> (&UN)[TY], const Pair<R> (&KB)[TY],
+                                                   const Pair<R> (&KC)[TY], const Pair<R> (&KA)[TY], Pair<R> (&KN)[TY])
+{
+    if (load_next) {
+        fu.load_plane(z + 2, UN);
+        fk.load_plane(z + 2, KN);
+    }
+    const long roff = (long)z * fu.plane + (long)fu.y0 * fu.pitch + fu.x0;
+    const R *ru = fu.in + roff;
+    const R *rk = fk.in + roff;
+    const Pair<R> hnu = fu.pair_at(fu.row(fu.y0 - 1, z));
+    const Pair<R> hsu = fu.pair_at(fu.row(fu.y0 + TY, z));
+    const Pair<R> hnk = fk.pair_at(fk.row(fk.y0 - 1, z));
+    const Pair<R> hsk = fk.pair_at(fk.row(fk.y0 + TY, z));
+    R *o = fu.out + roff;
+#pragma unroll
+    for (int j = 0; j < TY; ++j) {
+        R wu = shfl_up1(UC[j].b);
+        R eu = shfl_down1(UC[j].a);
+        R wk = shfl_up1(KC[j].b);
+        R ek = shfl_down1(KC[j].a);
+        if (fu.lane == 0) {
+            wu = fu.west(ru + j * fu.pitch);
+            wk = fk.west(rk + j * fk.pitch);
+        }
+        if (fu.lane == 31) {
+            eu = fu.east(ru + j * fu.pitch);
+            ek = fk.east(rk + j * fk.pitch);
+        }
+        const Pair<R> nu = (j == 0) ? hnu : UC[j - 1];
+        const Pair<R> su = (j == TY - 1) ? hsu : UC[j + 1];
+        const Pair<R> nk = (j == 0) ? hnk : KC[j - 1];
+        const Pair<R> sk = (j == TY - 1) ? hsk : KC[j + 1];
+        const R o0 = VarCoef<R>::apply(UC[j].a, KC[j].a, wu, wk, UC[j].b, KC[j].b, nu.a, nk.a, su.a, sk.a, UB[j].a, KB[j].a,
+                                       UA[j].a, KA[j].a);
+        const R o1 = VarCoef<R>::apply(UC[j].b, KC[j].b, UC[j].a, KC[j].a, eu, ek, nu.b, nk.b, su.b, sk.b, UB[j].b, KB[j].b,
+                                       UA[j].b, KA[j].b);
+        st_pair(o + j * fu.pitch, o0, o1);
+    }
+}
+
+template<typename R, int TY>
+__global__ void __launch_bounds__(64)
+varcoef_pair_kernel(View<const R> u, View<const R> k, View<R> out, int periodic, R edgeU, R edgeK, int zchunk)
+{
+    const int lane = threadIdx.x;
+    const int xb = blockIdx.x * 64;
+    const int x0 = xb + 2 * lane;
+    const int y0 = (blockIdx.y * blockDim.y + threadIdx.y) * TY;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, u.nz);
+    if (y0 >= u.ny) return;   // warp-uniform
+
+    if (xb + 64 <= u.nx && y0 + TY <= u.ny) {
+        PairFrame<R, TY> fu, fk;
+        fu.in = u.p;
+        fu.out = out.p;
+        fu.pitch = u.pitch;
+        fu.plane = u.pitch * u.ny;
+        fu.nx = u.nx;
+        fu.ny = u.ny;
+        fu.nz = u.nz;
+        fu.periodic = periodic;
+        fu.x0 = x0;
+        fu.y0 = y0;
+        fu.lane = lane;
+        fu.edge = edgeU;
+        fk = fu;
+        fk.in = k.p;
+        fk.edge = edgeK;
+        Pair<R> U0[TY], U1[TY], U2[TY], U3[TY], K0[TY], K1[TY], K2[TY], K3[TY];
+        fu.load_plane(z0 - 1, U0);
+        fu.load_plane(z0, U1);
+        fu.load_plane(z0 + 1, U2);
+        fk.load_plane(z0 - 1, K0);
+        fk.load_plane(z0, K1);
+        fk.load_plane(z0 + 1, K2);
+        for (int z = z0; z < z1; z += 4) {
+            varcoef_pair_plane<R, TY>(fu, fk, z, z + 1 < z1, U0, U1, U2, U3, K0, K1, K2, K3);
+            if (z + 1 >= z1) break;
+            varcoef_pair_plane<R, TY>(fu, fk, z + 1, z + 2 < z1, U1, U2, U3, U0, K1, K2, K3, K0);
+            if (z + 2 >= z1) break;
+            varcoef_pair_plane<R, TY>(fu, fk, z + 2, z + 3 < z1, U2, U3, U0, U1, K2, K3, K0, K1);
+            if (z + 3 >= z1) break;
+            varcoef_pair_plane<R, TY>(fu, fk, z + 3, z + 4 < z1, U3, U0, U1, U2, K3, K0, K1, K2);
+        }
+        return;
+    }
+
+    // partial footprint: per-cell loads
+    for (int z = z0; z < z1; ++z) {
+#pragma unroll
+        for (int j = 0; j < TY; ++j) {
+            const int y = y0 + j;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int x = x0 + h;
+                if (x < u.nx && y < u.ny) {
+                    out.at(x, y, z) = VarCoef<R>::apply(
+                        u.at(x, y, z), k.at(x, y, z),
+                        load_any(u, x - 1, y, z, periodic, edgeU), load_any(k, x - 1, y, z, periodic, edgeK),
+                        load_any(u, x + 1, y, z, periodic, edgeU), load_any(k, x + 1, y, z, periodic, edgeK),
+                        load_any(u, x, y - 1, z, periodic, edgeU), load_any(k, x, y - 1, z, periodic, edgeK),
+                        load_any(u, x, y + 1, z, periodic, edgeU), load_any(k, x, y + 1, z, periodic, edgeK),
+                        load_any(u, x, y, z - 1, periodic, edgeU), load_any(k, x, y, z - 1, periodic, edgeK),
+                        load_any(u, x, y, z + 1, periodic, edgeU), load_any(k, x, y, z + 1, periodic, edgeK));
+                }
+            }
+        }
+    }
+}
+
 void launch_varcoef(Grid& g, int steps)
 {
+    if (g.variant != 1) {
+        // two rows per warp: u and k both rotate through four planes
+        const int VC_TY = 2;
+        int zchunk = 1;
+        const dim3 grid = pair_grid(g, VC_TY, &zchunk);
+        for (int s = 0; s < steps; ++s) {
+            if (g.desc.cell == LGD_CELL_VARCOEF_F32) {
+                varcoef_pair_kernel<float, VC_TY><<<grid, dim3(32, PAIR_WY), 0, g.stream>>>(
+                    cmview<float>(g, 0, 0), cmview<float>(g, 1, 0), mview<float>(g, 0, 1), g.desc.periodic,
+                    (float)g.desc.edge[0], (float)g.desc.edge[1], zchunk);
+            } else {
+                varcoef_pair_kernel<double, VC_TY><<<grid, dim3(32, PAIR_WY), 0, g.stream>>>(
+                    cmview<double>(g, 0, 0), cmview<double>(g, 1, 0), mview<double>(g, 0, 1), g.desc.periodic,
+                    g.desc.edge[0], g.desc.edge[1], zchunk);
+            }
+            check_launch("varcoef");
+            ++g.launches;
+            g.cur = 1 - g.cur;
+        }
+        return;
+    }
     int zchunk = 1;
     dim3 grid = zmarch_grid(g, &zchunk);
     dim3 block(SBX, SBY);

@@ -297,6 +297,33 @@ def test_varcoef_f32_error_against_fp64():
     assert rel_l2 < 1e-6, rel_l2
 
 
+@pytest.mark.parametrize("shape", [(8, 12, 64), (20, 10, 128), (5, 7, 130), (3, 2, 64), (66, 4, 192)])
+def test_varcoef_f64_wide_grids_bit_exact(shape):
+    """Grids whose x extent fills 64-wide warps run the register kernel's
+    vector path (wrap decisions per row and plane)."""
+    nz, ny, nx = shape
+    rng = np.random.default_rng(nx * ny + nz)
+    u0 = rng.random(shape)
+    k = 0.02 + 0.13 * rng.random(shape)
+    out = run_grid(lgd.CELL_VARCOEF_F64, [u0, k], 9, periodic=7)
+    np.testing.assert_array_equal(out, oracle.varcoef(u0, k, 9))
+
+
+def test_varcoef_f32_register_kernel_equals_shared_memory_kernel():
+    u0, k = workloads.varcoef_fields(64, seed=3, length=8.0)
+    res = []
+    for variant in (0, 1):
+        with lgd.Grid(lgd.CELL_VARCOEF_F32, u0.shape, periodic=7) as g:
+            _set_variant(g, variant)
+            g.upload(0, u0.astype(np.float32))
+            g.upload(1, k.astype(np.float32))
+            g.step(12)
+            res.append(g.download(0).astype(np.float64))
+    ref = oracle.varcoef(u0, k, 12)
+    for r in res:
+        assert np.linalg.norm(r - ref) / np.linalg.norm(ref) < 1e-6
+
+
 # ------------------------------------------ kernel variants and fast paths
 def _set_variant(g, v):
     fn = lgd.lib().lgd_gpu_set_variant
