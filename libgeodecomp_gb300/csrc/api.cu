@@ -159,6 +159,24 @@ static void check_device_error(Grid& g)
     }
 }
 
+// Device staging buffer of the handle for conversions at the boundary,
+// allocated on first use and grown when needed (kept until destroy, so
+// repeated uploads and downloads do not allocate).
+static double *staging(Grid& g, size_t bytes)
+{
+    if (bytes > g.stage_bytes) {
+        if (g.d_stage) {
+            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            cudaFree(g.d_stage);
+            g.d_stage = nullptr;
+            g.stage_bytes = 0;
+        }
+        LGD_CHECK_CUDA(cudaMalloc(&g.d_stage, bytes));
+        g.stage_bytes = bytes;
+    }
+    return (double *)g.d_stage;
+}
+
 static Grid& grid_of(lgd_handle *h)
 {
     LGD_REQUIRE(h != nullptr, LGD_ERR_INVALID, "null handle");
@@ -325,6 +343,7 @@ int lgd_gpu_destroy(lgd_handle *h)
         if (g.d_streak_prefix) cudaFree(g.d_streak_prefix);
         if (g.d_partials) cudaFree(g.d_partials);
         if (g.d_err) cudaFree(g.d_err);
+        if (g.d_stage) cudaFree(g.d_stage);
         cudaStreamDestroy(g.stream);
         delete h;
     });
@@ -343,8 +362,7 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
         if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
             // stage the doubles on the device, find max |value| there, then
             // convert into the pitched fixed-point buffer
-            double *tmp = nullptr;
-            LGD_CHECK_CUDA(cudaMallocAsync(&tmp, n * 8 + 8 * 1024, g.stream));
+            double *tmp = staging(g, n * 8 + 8 * 1024);
             double *partial = tmp + n;
             LGD_CHECK_CUDA(cudaMemcpyAsync(tmp, host, n * 8, cudaMemcpyHostToDevice, g.stream));
             absmax_kernel<<<1024, 256, 0, g.stream>>>(tmp, (long long)n, partial);
@@ -355,18 +373,13 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
             double m = std::fabs(g.desc.edge[0]);
             for (int i = 0; i < 1024; ++i) m = std::fmax(m, hpart[i]);
-            if (!std::isfinite(m)) {
-                cudaFreeAsync(tmp, g.stream);
-                cudaStreamSynchronize(g.stream);
-                throw Error(LGD_ERR_INVALID, "grid holds a non-finite value");
-            }
+            LGD_REQUIRE(std::isfinite(m), LGD_ERR_INVALID, "grid holds a non-finite value");
             raise_fix_exp(g, exp_bound(m));
             long long *dst = (long long *)member_buf(g, member, which);
             const size_t pitch = g.pitch_bytes[0] / 8;
             to_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(tmp, dst, g.desc.nx, (long long)rows, (long long)pitch, g.fix_exp);
             check_launch("to fixed point");
             ++g.launches;
-            LGD_CHECK_CUDA(cudaFreeAsync(tmp, g.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
             return;
         }
@@ -388,15 +401,13 @@ int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t by
         LGD_REQUIRE(bytes == n * helem, LGD_ERR_INVALID, "byte count does not match the grid");
         const size_t rows = (size_t)g.desc.ny * g.desc.nz;
         if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
-            double *tmp = nullptr;
-            LGD_CHECK_CUDA(cudaMallocAsync(&tmp, n * 8, g.stream));
+            double *tmp = staging(g, n * 8);
             const long long *src = (const long long *)member_buf(g, member, which);
             const size_t pitch = g.pitch_bytes[0] / 8;
             from_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(src, tmp, g.desc.nx, (long long)rows, (long long)pitch, g.fix_exp);
             check_launch("from fixed point");
             ++g.launches;
             LGD_CHECK_CUDA(cudaMemcpyAsync(host, tmp, n * 8, cudaMemcpyDeviceToHost, g.stream));
-            LGD_CHECK_CUDA(cudaFreeAsync(tmp, g.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
             check_device_error(g);
             return;

@@ -103,6 +103,8 @@ struct Grid {
     bool tmap_ready[2];
     void *tmap_base[2];
     int *d_err;
+    void *d_stage;          // conversion staging at the boundary (fixed-point grids)
+    size_t stage_bytes;
 };
 
 bool tma_applicable(const Grid& g);
