@@ -15,7 +15,10 @@ grid (1 GiB per buffer) is larger than L2, so every step streams from HBM.
 
 Other workloads (--workload): gol_u8_8192 (Game of Life 8192^2 torus),
 sell_f64_4m (SELL-C-sigma diffusion, 4,194,304 nodes, C=32, sigma=256),
-jacobi7_f64_ieee_512 (the bit-exact IEEE FP64 kernel alone).
+jacobi7_f64_ieee_512 (the bit-exact IEEE FP64 kernel alone),
+lbm_d3q19_ensemble_512 (512 uneven D3Q19 cavities, one persistent launch per
+step), varcoef_f32_256 (variable-coefficient diffusion, 256^3 FP32 torus);
+--surrogate runs the learned-surrogate time-to-solution benchmark.
 
 --impl reference times the reference's CPU algorithm on this machine's host
 cores: the C restatement in oracle/ (the reference itself is not built on
@@ -267,6 +270,50 @@ class SellWorkload:
         self.g.close()
 
 
+class VarcoefWorkload:
+    """Variable-coefficient diffusion u' = u + sum_f 0.5 (k_c + k_n)(u_n - u_c)
+    on a 256^3 FP32 torus: u0 a Gaussian random field on [0, 1], k a
+    separate one on [0.02, 0.15] (length 16) - the plain stencil the learned
+    surrogate is measured against, to t = 4096."""
+    run_steps = 4096
+    bytes_per_unit = 12      # u read, k read, u written (FP32)
+
+    def __init__(self, edge: int = 256):
+        from libgeodecomp_gb300 import lgd, workloads
+        self.lgd = lgd
+        self.shape = (edge, edge, edge)
+        self.name = "varcoef_f32_%d" % edge
+        self.metric = "variable-coefficient diffusion GLUPS"
+        self.unit = "GLUPS"
+        self.units = int(np.prod(self.shape))
+        self.dtype = "f32"
+        self.u0, kappa = workloads.varcoef_fields(edge, seed=42, length=16.0)
+        self.g = lgd.Grid(lgd.CELL_VARCOEF_F32, self.shape, periodic=7)
+        self.g.upload(0, self.u0)
+        self.g.upload(1, kappa)
+        self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "torus", "cells": self.units,
+                       "kappa": "GRF length 16 mapped to [0.02, 0.15]",
+                       "l2": "u, k and u' (192 MiB) larger than L2; no flush between steps"}
+
+    stream = JacobiWorkload.stream
+    step = JacobiWorkload.step
+    sync = JacobiWorkload.sync
+    launches = JacobiWorkload.launches
+    close = JacobiWorkload.close
+
+    def host_buffers(self, torch):
+        hin = torch.empty(self.units * 4, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
+        hout = torch.empty(self.units * 4, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
+        hin[:] = self.u0.reshape(-1)
+        return hin.reshape(self.shape), hout.reshape(self.shape)
+
+    def e2e_run(self, hin, hout):
+        self.g.upload(0, hin)
+        self.g.step(self.run_steps)
+        self.g.download(0, out=hout)
+        return hin.nbytes, hout.nbytes
+
+
 class LbmWorkload:
     """512 D3Q19 lid-driven cavities, edges uniform in {32..192}, omega
     uniform in [1.0, 1.9), lid 0.05, FP32; one persistent launch per step,
@@ -339,10 +386,17 @@ def make_workload(name, size=512, lbm_instances=512, lbm_edge_max=192, lbm_tune=
         return GoLWorkload()
     if name == "sell_f64_4m":
         return SellWorkload()
+    if name == "varcoef_f32_256":
+        return VarcoefWorkload(256)
     raise ValueError(name)
 
 
-WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "gol_u8_8192", "sell_f64_4m", "lbm_d3q19_ensemble_512"]
+WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "gol_u8_8192", "sell_f64_4m", "lbm_d3q19_ensemble_512",
+                  "varcoef_f32_256"]
+METRICS = {"gol_u8_8192": "Game of Life GLUPS", "sell_f64_4m": "SELL-C-sigma diffusion GB/s and s/step",
+           "lbm_d3q19_ensemble_512": "D3Q19 ensemble GLUPS (one persistent launch per step)",
+           "varcoef_f32_256": "variable-coefficient diffusion GLUPS"}
+DTYPES = {"gol_u8_8192": "u8", "lbm_d3q19_ensemble_512": "f32", "varcoef_f32_256": "f32"}
 
 
 # ------------------------------------------------------------------ helpers
@@ -492,6 +546,9 @@ def cpu_stepper(name):
         s = oracle.sell_build(n, rp, col, w, 32, 256)
         x = workloads.sell_values(n, seed=42)[s["perm"]]
         return n, x, lambda a, k: oracle.sell_diffusion(s, 32, a, k)
+    if name == "varcoef_f32_256":
+        u0, kappa = workloads.varcoef_fields(256, seed=42, length=16.0)
+        return u0.size, u0, lambda a, k: oracle.varcoef(a, kappa, k)
     raise ValueError(name)
 
 
@@ -523,12 +580,11 @@ def run_reference(args, world, rank):
     state = fn(state, args.steps)
     dt = time.perf_counter() - t0
     value = units * args.steps / dt / 1e9
-    w_metric = JACOBI_METRIC if args.workload.startswith("jacobi7") else (
-        "Game of Life GLUPS" if args.workload == "gol_u8_8192" else "SELL-C-sigma diffusion GB/s and s/step")
+    w_metric = METRICS.get(args.workload, JACOBI_METRIC)
     line = {
         "metric": w_metric, "value": round(value, 4), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u8" if args.workload == "gol_u8_8192" else "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPES.get(args.workload, "f64"),
         "data": "synthetic (seeded SplitMix64)", "config": {"workload": args.workload},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": oracle.max_threads(), "kind": "port",

@@ -167,7 +167,12 @@ int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
  * otherwise variant 5; 1 shared-memory plane tiles loaded by the threads;
  * 2 one cell per lane in registers; 3 / 4 / 5 two cells per lane, 8 / 2 / 4
  * rows per warp, marching in z with register rotation and warp shuffles.
- * For tuning and comparison. */
+ * Var-coef cells: 0 (default) for FP32 TMA-staged planes of u and k, wrapped
+ * neighbours copied into their own areas (3D grids whose non-wrapping axes
+ * have zero edge values and, when x wraps, rows of a multiple of 16 bytes),
+ * otherwise (and for FP64) variant 2; 1 shared-memory plane tiles; 2 .. 5
+ * two cells per lane in registers.  6: the TMA kernel wherever it applies
+ * (either cell family), else the default.  For tuning and comparison. */
 int lgd_gpu_set_variant(lgd_handle *h, int variant);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or

@@ -79,6 +79,12 @@ int lgd_sell_synchronize(lgd_sell *h);
 int lgd_sell_stream(lgd_sell *h, void **stream);
 int lgd_sell_launch_count(lgd_sell *h, uint64_t *count);
 
+/* Kernel variant (all give identical results): 0 = default, software
+ * pipelined four slots deep (matrix entries of the next slots load while
+ * the x gathers of the current ones are in flight); 1 = two slots per
+ * iteration, no pipelining; 2 = pipelined two slots deep. */
+int lgd_sell_set_variant(lgd_sell *h, int variant);
+
 #ifdef __cplusplus
 }
 #endif

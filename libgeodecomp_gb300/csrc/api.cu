@@ -636,7 +636,7 @@ int lgd_gpu_set_variant(lgd_handle *h, int variant)
 {
     return guard([&] {
         Grid& g = grid_of(h);
-        LGD_REQUIRE(variant >= 0 && variant <= 5, LGD_ERR_INVALID, "variant must lie in [0, 5]");
+        LGD_REQUIRE(variant >= 0 && variant <= 6, LGD_ERR_INVALID, "variant must lie in [0, 6]");
         g.variant = variant;
     });
 }

@@ -499,7 +499,7 @@ static void launch_zcol(Grid& g, View<const typename CELL::T> in, View<typename 
 
 void launch_jacobi7(Grid& g, int steps)
 {
-    if (g.variant == 0 && tma_applicable(g)) {
+    if ((g.variant == 0 || g.variant == 6) && tma_applicable(g)) {
         for (int s = 0; s < steps; ++s) launch_jacobi7_tma(g);
         return;
     }
@@ -671,6 +671,13 @@ varcoef_pair_kernel(View<const R> u, View<const R> k, View<R> out, int periodic,
 
 void launch_varcoef(Grid& g, int steps)
 {
+    // default: the TMA kernel for FP32 cells (HBM-bound); FP64 cells are
+    // bound by the FP64 rate, where the register kernel measured faster
+    const bool tma = (g.variant == 6) || (g.variant == 0 && g.desc.cell == LGD_CELL_VARCOEF_F32);
+    if (tma && varcoef_tma_applicable(g)) {
+        for (int s = 0; s < steps; ++s) launch_varcoef_tma(g);
+        return;
+    }
     if (g.variant != 1) {
         // two rows per warp: u and k both rotate through four planes
         const int VC_TY = 2;

@@ -224,6 +224,196 @@ jacobi7_tma_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T 
     }
 }
 
+// Variable-coefficient diffusion with the same plane ring, carrying u and k
+// and supporting wrapping axes.  Per plane and field the CTA copies the
+// main box ((64 + 2 pad) x 18 cells, out-of-bounds cells zero) and, where
+// an axis wraps and the tile touches the domain's edge, the wrapped
+// neighbours into separate areas of the slot: the row y = ny - 1 (north of
+// y = 0), the row y = 0 (south of y = ny - 1), a 16-byte column ending at
+// x = nx - 1 (west of x = 0) and one starting at x = 0 (east of x = nx - 1).
+// Wrapped z planes come from the plane index modulo nz.  Rows and columns
+// are picked warp-uniformly (per row) or per lane when the compute reads
+// its neighbours.  Traffic: u and k read once, u written once (12 B per
+// cell for FP32).
+namespace vc {
+
+template<typename T>
+struct Lay {
+    typedef Box<T> B;
+    static constexpr int MAIN = (B::W * B::H * (int)sizeof(T) + 127) / 128 * 128;
+    static constexpr int ROW = (B::W * (int)sizeof(T) + 127) / 128 * 128;
+    static constexpr int COL = (B::XPAD * B::H * (int)sizeof(T) + 127) / 128 * 128;
+    // field block: main, north row, south row, west column, east column
+    static constexpr int ROWN = MAIN;
+    static constexpr int ROWS_ = MAIN + ROW;
+    static constexpr int COLW = MAIN + 2 * ROW;
+    static constexpr int COLE = MAIN + 2 * ROW + COL;
+    static constexpr int FIELD = MAIN + 2 * ROW + 2 * COL;
+    static constexpr int SLOT = 2 * FIELD;
+};
+
+// tensor maps of one step: [field][main, row, col]
+struct Maps {
+    CUtensorMap m[2][3];
+};
+
+}  // namespace vc
+
+template<typename R>
+__global__ void __launch_bounds__(THREADS)
+varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, long pitch, int nx, int ny, int nz,
+                   int periodic, int zchunk, int *err)
+{
+    typedef Box<R> B;
+    typedef vc::Lay<R> Y;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[S];
+    __shared__ int s_fail;
+    __shared__ int s_issued;
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    const int x0 = blockIdx.x * TX;
+    const int y0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, nz);
+    if (z0 >= z1) return;
+    const int nplanes = (z1 - z0) + 2;
+    const bool xw = (periodic & 1) != 0;
+    const bool yw = (periodic & 2) != 0;
+    const bool zw = (periodic & 4) != 0;
+    // which wrapped areas this tile needs (uniform across the CTA)
+    const bool need_n = yw && y0 == 0;
+    const bool need_s = yw && y0 + TY >= ny;
+    const bool need_w = xw && x0 == 0;
+    const bool need_e = xw && x0 + TX >= nx;
+    const uint32_t bytes = 2u * (uint32_t)(B::W * B::H * sizeof(R) + (need_n + need_s) * B::W * sizeof(R) +
+                                           (need_w + need_e) * B::XPAD * B::H * sizeof(R));
+
+    auto issue = [&](int q) {
+        const uint32_t bar = smem_addr(&bars[q % S]);
+        int z = z0 - 1 + q;
+        if (zw) z = (z + nz) % nz;
+        mbar_expect_tx(bar, bytes);
+        unsigned char *slot = smem + (q % S) * Y::SLOT;
+#pragma unroll
+        for (int f = 0; f < 2; ++f) {
+            unsigned char *fb = slot + f * Y::FIELD;
+            tma_load_3d(smem_addr(fb), &maps.m[f][0], x0 - B::XPAD, y0 - 1, z, bar);
+            if (need_n) tma_load_3d(smem_addr(fb + Y::ROWN), &maps.m[f][1], x0 - B::XPAD, ny - 1, z, bar);
+            if (need_s) tma_load_3d(smem_addr(fb + Y::ROWS_), &maps.m[f][1], x0 - B::XPAD, 0, z, bar);
+            if (need_w) tma_load_3d(smem_addr(fb + Y::COLW), &maps.m[f][2], nx - B::XPAD, y0 - 1, z, bar);
+            if (need_e) tma_load_3d(smem_addr(fb + Y::COLE), &maps.m[f][2], 0, y0 - 1, z, bar);
+        }
+    };
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) mbar_init(smem_addr(&bars[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+        const int first = min(D, nplanes - 1);
+        for (int q = 0; q <= first; ++q) issue(q);
+        s_issued = first + 1;
+    }
+    __syncthreads();
+
+    int waited = -1;
+    for (int q = 0; q < 2; ++q) {
+        if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1)) s_fail = 1;
+        waited = q;
+    }
+
+    const int lx = 2 * lane;
+    const int gx = x0 + lx;
+    const int rw = warp * ROWS;
+    const long plane = pitch * ny;
+    // element offsets (bytes) inside a field block
+    auto mo = [&](int ly, int lxx) { return ((ly + 1) * B::W + lxx + B::XPAD) * (int)sizeof(R); };
+    auto ld = [&](const unsigned char *p) { return *reinterpret_cast<const R *>(p); };
+
+    for (int z = z0; z < z1; ++z) {
+        const int q = z - z0 + 1;
+        __syncthreads();
+        if (s_fail) break;
+        if (tid == 0 && q + D < nplanes) {
+            issue(q + D);
+            s_issued = q + D + 1;
+        }
+        if (!mbar_wait_bounded(smem_addr(&bars[(q + 1) % S]), ((q + 1) / S) & 1)) {
+            s_fail = 1;
+            continue;
+        }
+        waited = q + 1;
+
+        const unsigned char *sb = smem + ((q - 1) % S) * Y::SLOT;
+        const unsigned char *sc = smem + (q % S) * Y::SLOT;
+        const unsigned char *st = smem + ((q + 1) % S) * Y::SLOT;
+        R *orow = out + (long)z * plane + (long)(y0 + rw) * pitch + gx;
+#pragma unroll
+        for (int j = 0; j < ROWS; ++j) {
+            const int ly = rw + j;
+            const int gy = y0 + ly;
+            if (gy >= ny) break;                        // warp-uniform
+            R c[2][2], nb[2][2], sb2[2][2], tp[2][2], bt[2][2], we[2], ea[2];
+#pragma unroll
+            for (int f = 0; f < 2; ++f) {
+                const unsigned char *cf = sc + f * Y::FIELD;
+                lds_pair<R>(cf + mo(ly, lx), c[f][0], c[f][1]);
+                if (need_n && gy == 0) {
+                    lds_pair<R>(cf + Y::ROWN + (lx + B::XPAD) * (int)sizeof(R), nb[f][0], nb[f][1]);
+                } else {
+                    lds_pair<R>(cf + mo(ly - 1, lx), nb[f][0], nb[f][1]);
+                }
+                if (need_s && gy == ny - 1) {
+                    lds_pair<R>(cf + Y::ROWS_ + (lx + B::XPAD) * (int)sizeof(R), sb2[f][0], sb2[f][1]);
+                } else {
+                    lds_pair<R>(cf + mo(ly + 1, lx), sb2[f][0], sb2[f][1]);
+                }
+                lds_pair<R>(st + f * Y::FIELD + mo(ly, lx), tp[f][0], tp[f][1]);
+                lds_pair<R>(sb + f * Y::FIELD + mo(ly, lx), bt[f][0], bt[f][1]);
+                // west of the lane's first cell, east of its second (or of
+                // the first when the second lies beyond nx)
+                we[f] = (need_w && gx == 0) ? ld(cf + Y::COLW + ((ly + 1) * B::XPAD + B::XPAD - 1) * (int)sizeof(R))
+                                            : ld(cf + mo(ly, lx - 1));
+                const int ex = (gx + 1 < nx) ? gx + 2 : gx + 1;     // global x of the east neighbour
+                ea[f] = (need_e && ex == nx) ? ld(cf + Y::COLE + (ly + 1) * B::XPAD * (int)sizeof(R))
+                                             : ld(cf + mo(ly, ex - x0));
+            }
+            if (gx >= nx) continue;
+            R *o = orow + (long)j * pitch;
+            if (gx + 1 < nx) {
+                const R o0 = VarCoef<R>::apply(c[0][0], c[1][0], we[0], we[1], c[0][1], c[1][1], nb[0][0], nb[1][0],
+                                               sb2[0][0], sb2[1][0], bt[0][0], bt[1][0], tp[0][0], tp[1][0]);
+                const R o1 = VarCoef<R>::apply(c[0][1], c[1][1], c[0][0], c[1][0], ea[0], ea[1], nb[0][1], nb[1][1],
+                                               sb2[0][1], sb2[1][1], bt[0][1], bt[1][1], tp[0][1], tp[1][1]);
+                if (sizeof(R) == 8) {
+                    longlong2 v;
+                    v.x = *reinterpret_cast<const long long *>(&o0);
+                    v.y = *reinterpret_cast<const long long *>(&o1);
+                    *reinterpret_cast<longlong2 *>(o) = v;
+                } else {
+                    int2 v;
+                    v.x = *reinterpret_cast<const int *>(&o0);
+                    v.y = *reinterpret_cast<const int *>(&o1);
+                    *reinterpret_cast<int2 *>(o) = v;
+                }
+            } else {
+                o[0] = VarCoef<R>::apply(c[0][0], c[1][0], we[0], we[1], ea[0], ea[1], nb[0][0], nb[1][0], sb2[0][0],
+                                         sb2[1][0], bt[0][0], bt[1][0], tp[0][0], tp[1][0]);
+            }
+        }
+    }
+
+    __syncthreads();
+    if (s_fail) {
+        if (tid == 0) atomicExch(err, 1);
+        for (int q = waited + 1; q < s_issued; ++q) {
+            if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1)) break;
+        }
+    }
+}
+
 // -------------------------------------------------------------- host side
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -247,13 +437,14 @@ static EncodeTiledFn encode_fn()
 }
 
 template<typename T>
-static void encode(CUtensorMap *map, void *base, const Grid& g, CUtensorMapDataType dt)
+static void encode(CUtensorMap *map, void *base, const Grid& g, CUtensorMapDataType dt, int member = 0,
+                   int box_w = Box<T>::W, int box_h = Box<T>::H)
 {
     EncodeTiledFn fn = encode_fn();
     LGD_REQUIRE(fn != nullptr, LGD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[3] = {(cuuint64_t)g.desc.nx, (cuuint64_t)g.desc.ny, (cuuint64_t)g.desc.nz};
-    const cuuint64_t strides[2] = {(cuuint64_t)g.pitch_bytes[0], (cuuint64_t)g.pitch_bytes[0] * g.desc.ny};
-    const cuuint32_t box[3] = {(cuuint32_t)Box<T>::W, (cuuint32_t)Box<T>::H, 1};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.pitch_bytes[member], (cuuint64_t)g.pitch_bytes[member] * g.desc.ny};
+    const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -309,6 +500,69 @@ static void launch_tma_typed(Grid& g, CUtensorMapDataType dt)
     tmak::jacobi7_tma_kernel<CELL><<<dim3(bx, by, zsplit), tmak::THREADS, smem, g.stream>>>(
         *map, (T *)g.m[0].buf[1 - src], (long)(g.pitch_bytes[0] / sizeof(T)), g.desc.nx, g.desc.ny, g.desc.nz, zchunk,
         g.d_err);
+}
+
+// The var-coef TMA kernel: 3D grids whose non-wrapping axes have zero edge
+// values for u and k, and - when x wraps - rows whose length is a multiple
+// of 16 bytes (the west column's copy starts at x = nx - 16 / sizeof(T)).
+bool varcoef_tma_applicable(const Grid& g)
+{
+    if (g.desc.dim != 3) return false;
+    const int elem = (g.desc.cell == LGD_CELL_VARCOEF_F32) ? 4 : 8;
+    if (g.desc.cell != LGD_CELL_VARCOEF_F32 && g.desc.cell != LGD_CELL_VARCOEF_F64) return false;
+    if (g.desc.periodic != 7 && (g.desc.edge[0] != 0.0 || g.desc.edge[1] != 0.0)) return false;
+    if ((g.desc.periodic & 1) && ((long long)g.desc.nx * elem) % 16 != 0) return false;
+    return g.pitch_bytes[0] == g.pitch_bytes[1];
+}
+
+template<typename R>
+static void launch_varcoef_tma_typed(Grid& g, CUtensorMapDataType dt)
+{
+    typedef tmak::Box<R> B;
+    const int src = g.cur;
+    void *ubuf = g.m[0].buf[src];
+    void *kbuf = g.m[1].buf[0];
+    tmak::vc::Maps *maps = reinterpret_cast<tmak::vc::Maps *>(g.vtmap[src]);
+    if (!g.vtmap_ready[src] || g.vtmap_base[src][0] != ubuf || g.vtmap_base[src][1] != kbuf) {
+        void *bases[2] = {ubuf, kbuf};
+        for (int f = 0; f < 2; ++f) {
+            tmak::encode<R>(&maps->m[f][0], bases[f], g, dt, f, B::W, B::H);
+            tmak::encode<R>(&maps->m[f][1], bases[f], g, dt, f, B::W, 1);
+            tmak::encode<R>(&maps->m[f][2], bases[f], g, dt, f, B::XPAD, B::H);
+        }
+        g.vtmap_ready[src] = true;
+        g.vtmap_base[src][0] = ubuf;
+        g.vtmap_base[src][1] = kbuf;
+    }
+    const int smem = tmak::S * tmak::vc::Lay<R>::SLOT;
+    static bool configured = false;
+    if (!configured) {
+        LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::varcoef_tma_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        configured = true;
+    }
+    const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
+    const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
+    const long long xy = (long long)bx * by;
+    // about four waves of three resident CTAs per SM
+    int zsplit = (int)((152LL * 12 + xy - 1) / xy);
+    zsplit = std::max(1, std::min(zsplit, (g.desc.nz + 15) / 16));
+    int zchunk = (g.desc.nz + zsplit - 1) / zsplit;
+    zsplit = (g.desc.nz + zchunk - 1) / zchunk;
+    tmak::varcoef_tma_kernel<R><<<dim3(bx, by, zsplit), tmak::THREADS, smem, g.stream>>>(
+        *maps, (R *)g.m[0].buf[1 - src], (long)(g.pitch_bytes[0] / sizeof(R)), g.desc.nx, g.desc.ny, g.desc.nz,
+        g.desc.periodic, zchunk, g.d_err);
+}
+
+void launch_varcoef_tma(Grid& g)
+{
+    if (g.desc.cell == LGD_CELL_VARCOEF_F32) {
+        launch_varcoef_tma_typed<float>(g, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+    } else {
+        launch_varcoef_tma_typed<double>(g, CU_TENSOR_MAP_DATA_TYPE_FLOAT64);
+    }
+    check_launch("varcoef tma");
+    ++g.launches;
+    g.cur = 1 - g.cur;
 }
 
 void launch_jacobi7_tma(Grid& g)

@@ -55,6 +55,7 @@ struct Lbm {
     cudaStream_t stream;
     cudaGraphExec_t graph;
     bool graph_valid;
+    bool idx32;         // every instance indexable with 32 bits (19 L^3 < 2^31)
     uint64_t launches;
 };
 
@@ -105,15 +106,15 @@ struct LbmArith<float> {
     static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
 };
 
-template<typename R, int I>
-__device__ __forceinline__ void pull_one(const R *__restrict__ src, long long n3, long long cell, int L, int x, int y,
+template<typename R, int I, typename IDX>
+__device__ __forceinline__ void pull_one(const R *__restrict__ src, IDX n3, IDX cell, int L, int x, int y,
                                          int z, R lid, R *f)
 {
     const int sx = x - Q<I>::ex;
     const int sy = y - Q<I>::ey;
     const int sz = z - Q<I>::ez;
     if ((unsigned)sx < (unsigned)L && (unsigned)sy < (unsigned)L && (unsigned)sz < (unsigned)L) {
-        f[I] = src[I * n3 + cell - (Q<I>::ex + (long long)Q<I>::ey * L + (long long)Q<I>::ez * L * L)];
+        f[I] = src[I * n3 + cell - (Q<I>::ex + (IDX)Q<I>::ey * L + (IDX)Q<I>::ez * L * L)];
     } else {
         const R w = (I == 0) ? (R)(1.0 / 3.0) : ((I < 7) ? (R)(1.0 / 18.0) : (R)(1.0 / 36.0));
         R v = src[Q<I>::opp * n3 + cell];
@@ -126,24 +127,23 @@ __device__ __forceinline__ void pull_one(const R *__restrict__ src, long long n3
     }
 }
 
-template<typename R, int I>
+template<typename R, int I, typename IDX>
 struct PullAll {
-    static __device__ __forceinline__ void run(const R *src, long long n3, long long cell, int L, int x, int y, int z,
-                                               R lid, R *f)
+    static __device__ __forceinline__ void run(const R *src, IDX n3, IDX cell, int L, int x, int y, int z, R lid, R *f)
     {
-        pull_one<R, I>(src, n3, cell, L, x, y, z, lid, f);
-        PullAll<R, I + 1>::run(src, n3, cell, L, x, y, z, lid, f);
+        pull_one<R, I, IDX>(src, n3, cell, L, x, y, z, lid, f);
+        PullAll<R, I + 1, IDX>::run(src, n3, cell, L, x, y, z, lid, f);
     }
 };
 
-template<typename R>
-struct PullAll<R, 19> {
-    static __device__ __forceinline__ void run(const R *, long long, long long, int, int, int, int, R, R *) {}
+template<typename R, typename IDX>
+struct PullAll<R, 19, IDX> {
+    static __device__ __forceinline__ void run(const R *, IDX, IDX, int, int, int, int, R, R *) {}
 };
 
 // BGK collision, operation order of the oracle's lgd_d3q19_collide
-template<typename R>
-__device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict__ dst, long long n3, long long cell)
+template<typename R, typename IDX>
+__device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict__ dst, IDX n3, IDX cell)
 {
     typedef LbmArith<R> A;
     R rho = f[0];
@@ -173,47 +173,55 @@ __device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict
     }
 }
 
-template<typename R>
+// Cells of rows [y0, y1) of plane z (contiguous in memory), the threads
+// first, first + stride, ... of the group taking cells in that order.  IDX
+// is the index type inside one instance: 32-bit when 19 L^3 < 2^31.
+template<typename R, typename IDX>
 __device__ __forceinline__ void lbm_item(const LbmInstance& in, const R *__restrict__ A, R *__restrict__ B, int z, int y0,
-                                         int y1)
+                                         int y1, unsigned first, unsigned stride)
 {
     const int L = in.L;
-    const long long n3 = (long long)L * L * L;
+    const IDX n3 = (IDX)L * L * L;
     const R *src = A + in.base;
     R *dst = B + in.base;
     const R omega = (sizeof(R) == 8) ? (R)in.omega : (R)in.omega_f;
     const R lid = (sizeof(R) == 8) ? (R)in.lid : (R)in.lid_f;
     const unsigned cells = (unsigned)(y1 - y0) * (unsigned)L;
-    for (unsigned c = threadIdx.x; c < cells; c += blockDim.x) {
+    for (unsigned c = first; c < cells; c += stride) {
         unsigned r = __umulhi(c, in.magic);
         if (r * (unsigned)L > c) --r;
         const int y = y0 + (int)r;
         const int x = (int)(c - r * (unsigned)L);
-        const long long cell = ((long long)z * L + y) * L + x;
+        const IDX cell = ((IDX)z * L + y) * L + x;
         R f[19];
-        PullAll<R, 0>::run(src, n3, cell, L, x, y, z, lid, f);
-        collide_store<R>(f, omega, dst, n3, cell);
+        PullAll<R, 0, IDX>::run(src, n3, cell, L, x, y, z, lid, f);
+        collide_store<R, IDX>(f, omega, dst, n3, cell);
     }
 }
 
-template<typename R>
+// Every warp pulls its own work items from the counter - no CTA barrier, so
+// a warp that finishes a short item starts the next at once - and claims
+// the next item before it processes the current one, which hides the
+// atomic's round trip.
+template<typename R, typename IDX>
 __global__ void lbm_persistent_kernel(const LbmInstance *__restrict__ inst, const int4 *__restrict__ items, int n_items,
                                       int *counter, const R *__restrict__ A, R *__restrict__ B)
 {
-    __shared__ int s_item;
-    while (true) {
-        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-        __syncthreads();
-        const int it = s_item;
-        __syncthreads();
-        if (it >= n_items) break;
+    const unsigned lane = threadIdx.x & 31u;
+    int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    while (it < n_items) {
+        int next = 0;
+        if (lane == 0) next = atomicAdd(counter, 1);
         const int4 w = items[it];
-        lbm_item<R>(inst[w.x], A, B, w.y, w.z, w.w);
+        lbm_item<R, IDX>(inst[w.x], A, B, w.y, w.z, w.w, lane, 32u);
+        it = __shfl_sync(0xffffffffu, next, 0);
     }
 }
 
 // one instance, one launch: the looped single-grid comparison
-template<typename R>
+template<typename R, typename IDX>
 __global__ void lbm_single_kernel(const LbmInstance *__restrict__ inst, int j, const R *__restrict__ A, R *__restrict__ B)
 {
     const LbmInstance in = inst[j];
@@ -221,7 +229,7 @@ __global__ void lbm_single_kernel(const LbmInstance *__restrict__ inst, int j, c
     const int rows_per_block = max(1, (int)(blockDim.x / in.L));
     const int y0 = blockIdx.x * rows_per_block;
     if (y0 >= in.L) return;
-    lbm_item<R>(in, A, B, z, y0, min(in.L, y0 + rows_per_block));
+    lbm_item<R, IDX>(in, A, B, z, y0, min(in.L, y0 + rows_per_block), threadIdx.x, blockDim.x);
 }
 
 template<typename R>
@@ -268,18 +276,44 @@ static void build_items(Lbm& e)
     e.n_items = (int)items.size();
 }
 
+// the persistent kernel for the ensemble's precision and index width
+static const void *persistent_fn(const Lbm& e)
+{
+    if (e.precision == 4) {
+        return e.idx32 ? (const void *)lbm_persistent_kernel<float, int> : (const void *)lbm_persistent_kernel<float, long long>;
+    }
+    return e.idx32 ? (const void *)lbm_persistent_kernel<double, int> : (const void *)lbm_persistent_kernel<double, long long>;
+}
+
 static void launch_step(Lbm& e, int which_counter, int src)
 {
     LGD_CHECK_CUDA(cudaMemsetAsync(e.d_counter + which_counter, 0, sizeof(int), e.stream));
     const int grid = e.sms * e.ctas_per_sm;
+    int *counter = e.d_counter + which_counter;
+    const void *a = e.buf[src];
+    void *b = e.buf[1 - src];
+    void *args[] = {&e.d_inst, &e.d_items, &e.n_items, &counter, &a, &b};
+    LGD_CHECK_CUDA(cudaLaunchKernel(persistent_fn(e), dim3(grid), dim3(e.threads), args, 0, e.stream));
+}
+
+static void launch_single(Lbm& e, int j, dim3 grid)
+{
+    const void *a = e.buf[e.cur];
+    void *b = e.buf[1 - e.cur];
     if (e.precision == 4) {
-        lbm_persistent_kernel<float><<<grid, e.threads, 0, e.stream>>>(
-            e.d_inst, e.d_items, e.n_items, e.d_counter + which_counter, (const float *)e.buf[src], (float *)e.buf[1 - src]);
+        if (e.idx32) {
+            lbm_single_kernel<float, int><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const float *)a, (float *)b);
+        } else {
+            lbm_single_kernel<float, long long><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const float *)a, (float *)b);
+        }
     } else {
-        lbm_persistent_kernel<double><<<grid, e.threads, 0, e.stream>>>(
-            e.d_inst, e.d_items, e.n_items, e.d_counter + which_counter, (const double *)e.buf[src], (double *)e.buf[1 - src]);
+        if (e.idx32) {
+            lbm_single_kernel<double, int><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const double *)a, (double *)b);
+        } else {
+            lbm_single_kernel<double, long long><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const double *)a, (double *)b);
+        }
     }
-    check_launch("lbm persistent");
+    check_launch("lbm single");
 }
 
 static void rebuild_graph(Lbm& e)
@@ -311,11 +345,7 @@ static void set_config(Lbm& e, int ty, int threads, int ctas)
                 "threads per CTA must be a power of two in [64, 1024]");
     LGD_REQUIRE(ctas >= 1 && ctas <= 32, LGD_ERR_INVALID, "CTAs per SM out of range");
     int max_ctas = 0;
-    if (e.precision == 4) {
-        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_ctas, lbm_persistent_kernel<float>, threads, 0));
-    } else {
-        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_ctas, lbm_persistent_kernel<double>, threads, 0));
-    }
+    LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_ctas, persistent_fn(e), threads, 0));
     LGD_REQUIRE(max_ctas >= 1, LGD_ERR_INVALID, "kernel does not fit with this many threads");
     ctas = std::min(ctas, max_ctas);   // a persistent grid never exceeds what is resident
     const bool items_change = (ty != e.ty) || e.d_items == nullptr;
@@ -376,6 +406,7 @@ int lgd_lbm_create(int count, const int32_t *edges, const double *omegas, double
         e->precision = precision;
         e->inst.resize(count);
         long long off = 0;
+        e->idx32 = true;
         for (int j = 0; j < count; ++j) {
             LGD_REQUIRE(edges[j] >= 2 && edges[j] <= 1024, LGD_ERR_RANGE, "instance edge must lie in [2, 1024]");
             LGD_REQUIRE(omegas[j] > 0.0 && omegas[j] < 2.0, LGD_ERR_RANGE, "omega must lie in (0, 2)");
@@ -390,6 +421,7 @@ int lgd_lbm_create(int count, const int32_t *edges, const double *omegas, double
             const long long n3 = (long long)edges[j] * edges[j] * edges[j];
             off += 19 * n3;
             e->total_cells += n3;
+            if (19 * n3 >= (1ll << 31)) e->idx32 = false;
             LGD_REQUIRE(n3 * 19 < (1ll << 31) * 16, LGD_ERR_RANGE, "instance too large");
         }
         e->total_elems = off;
@@ -449,15 +481,7 @@ int lgd_lbm_step_looped(lgd_lbm *h, int steps)
             for (int j = 0; j < e.count; ++j) {
                 const int L = e.inst[j].L;
                 const int rows = std::max(1, 256 / L);
-                dim3 grid((L + rows - 1) / rows, L);
-                if (e.precision == 4) {
-                    lbm_single_kernel<float><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const float *)e.buf[e.cur],
-                                                                         (float *)e.buf[1 - e.cur]);
-                } else {
-                    lbm_single_kernel<double><<<grid, 256, 0, e.stream>>>(e.d_inst, j, (const double *)e.buf[e.cur],
-                                                                          (double *)e.buf[1 - e.cur]);
-                }
-                check_launch("lbm single");
+                launch_single(e, j, dim3((L + rows - 1) / rows, L));
                 ++e.launches;
             }
             e.cur = 1 - e.cur;

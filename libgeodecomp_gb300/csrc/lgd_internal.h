@@ -105,10 +105,17 @@ struct Grid {
     int *d_err;
     void *d_stage;          // conversion staging at the boundary (fixed-point grids)
     size_t stage_bytes;
+    // var-coef TMA kernel: six tensor maps (u and k; main box, row, column)
+    // per u buffer and the buffers they were built for
+    alignas(64) unsigned char vtmap[2][6 * 128];
+    bool vtmap_ready[2];
+    void *vtmap_base[2][2];
 };
 
 bool tma_applicable(const Grid& g);
 void launch_jacobi7_tma(Grid& g);
+bool varcoef_tma_applicable(const Grid& g);
+void launch_varcoef_tma(Grid& g);
 
 // kernels, one entry per cell family (implemented in k_*.cu)
 void launch_jacobi7(Grid& g, int steps);

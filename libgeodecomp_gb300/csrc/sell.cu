@@ -47,6 +47,7 @@ struct Sell {
     void *d_x[2];           // rows_padded each
     int *d_perm;            // physical -> logical (n), or null
     int cur;
+    int variant;            // 0 = pipelined (default), 1 = two gathers per iteration, 2 = pipelined depth 2
     cudaStream_t stream;
     uint64_t launches;
 };
@@ -122,6 +123,68 @@ sell_diffusion_kernel(const int *__restrict__ chunk_offset, const int *__restric
     }
 }
 
+// Software-pipelined form: the matrix entries of slots k+D .. k+2D-1 are
+// loaded while the x gathers of slots k .. k+D-1 are in flight, so a
+// row's iterations cost one memory round trip each instead of a DRAM trip
+// followed by a dependent L2 trip.  Slots below the chunk length exist for
+// every lane of the chunk, lanes load only their own row's entries; the
+// sum runs in slot order, as in the kernel above.
+template<typename R, bool EXACT, int D>
+__global__ void __launch_bounds__(256)
+sell_diffusion_pipe_kernel(const int *__restrict__ chunk_offset, const int *__restrict__ row_length,
+                           const R *__restrict__ values, const int *__restrict__ column,
+                           const R *__restrict__ x, R *__restrict__ xn, int n, int C, int row_begin, int row_end)
+{
+    const int row = row_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= row_end) return;
+    const int chunk = row / C;
+    const long long base = (long long)chunk_offset[chunk] + (row - chunk * C);
+    const int len = row_length[row];
+    const R xr = x[row];
+    const R *v = values + base;
+    const int *c = column + base;
+    R w[D];
+    int cc[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        w[j] = (R)0;
+        cc[j] = 0;
+        if (j < len) {
+            w[j] = __ldg(v + (long long)j * C);
+            cc[j] = __ldg(c + (long long)j * C);
+        }
+    }
+    R acc = (R)0;
+    for (int k = 0; k < len; k += D) {
+        R g[D];
+#pragma unroll
+        for (int j = 0; j < D; ++j) g[j] = (k + j < len) ? __ldg(x + cc[j]) : (R)0;
+        R nw[D];
+        int nc[D];
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            nw[j] = (R)0;
+            nc[j] = 0;
+            if (k + D + j < len) {
+                nw[j] = __ldg(v + (long long)(k + D + j) * C);
+                nc[j] = __ldg(c + (long long)(k + D + j) * C);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            if (k + j < len) acc = madd<R, EXACT>(acc, g[j], w[j]);
+            w[j] = nw[j];
+            cc[j] = nc[j];
+        }
+    }
+    if (EXACT) {
+        xn[row] = (sizeof(R) == 8) ? (R)__dadd_rn(__dmul_rn(0.1, (double)xr), (double)acc)
+                                   : (R)__fadd_rn(__fmul_rn(0.1f, (float)xr), (float)acc);
+    } else {
+        xn[row] = (R)0.1 * xr + acc;
+    }
+}
+
 template<typename R>
 __global__ void permute_in_kernel(const double *logical, const int *perm, R *phys, int n)
 {
@@ -157,31 +220,45 @@ static void sell_free(Sell& s)
     if (s.stream) cudaStreamDestroy(s.stream);
 }
 
+template<typename R, bool EXACT>
+static void launch_sell_typed(Sell& s, int row_begin, int row_end)
+{
+    const int threads = 256;
+    const int blocks = (row_end - row_begin + threads - 1) / threads;
+    const R *x = (const R *)s.d_x[s.cur];
+    R *xn = (R *)s.d_x[1 - s.cur];
+    const R *vals = (const R *)s.d_values;
+    switch (s.variant) {
+    case 1:
+        sell_diffusion_kernel<R, EXACT><<<blocks, threads, 0, s.stream>>>(
+            s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        break;
+    case 2:
+        sell_diffusion_pipe_kernel<R, EXACT, 2><<<blocks, threads, 0, s.stream>>>(
+            s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        break;
+    default:
+        sell_diffusion_pipe_kernel<R, EXACT, 4><<<blocks, threads, 0, s.stream>>>(
+            s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+        break;
+    }
+}
+
 static void launch_sell(Sell& s, int row_begin, int row_end)
 {
     if (row_end <= row_begin) return;
-    const int threads = 256;
-    const int blocks = (row_end - row_begin + threads - 1) / threads;
     const bool exact = (s.flags & LGD_SELL_EXACT) != 0;
     if (s.precision == 8) {
-        const double *x = (const double *)s.d_x[s.cur];
-        double *xn = (double *)s.d_x[1 - s.cur];
         if (exact) {
-            sell_diffusion_kernel<double, true><<<blocks, threads, 0, s.stream>>>(
-                s.d_chunk_offset, s.d_row_length, (const double *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+            launch_sell_typed<double, true>(s, row_begin, row_end);
         } else {
-            sell_diffusion_kernel<double, false><<<blocks, threads, 0, s.stream>>>(
-                s.d_chunk_offset, s.d_row_length, (const double *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+            launch_sell_typed<double, false>(s, row_begin, row_end);
         }
     } else {
-        const float *x = (const float *)s.d_x[s.cur];
-        float *xn = (float *)s.d_x[1 - s.cur];
         if (exact) {
-            sell_diffusion_kernel<float, true><<<blocks, threads, 0, s.stream>>>(
-                s.d_chunk_offset, s.d_row_length, (const float *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+            launch_sell_typed<float, true>(s, row_begin, row_end);
         } else {
-            sell_diffusion_kernel<float, false><<<blocks, threads, 0, s.stream>>>(
-                s.d_chunk_offset, s.d_row_length, (const float *)s.d_values, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+            launch_sell_typed<float, false>(s, row_begin, row_end);
         }
     }
     check_launch("sell diffusion");
@@ -454,6 +531,15 @@ int lgd_sell_stream(lgd_sell *h, void **stream)
     return guard([&] {
         LGD_REQUIRE(stream != nullptr, LGD_ERR_INVALID, "null output");
         *stream = (void *)sell_of(h).stream;
+    });
+}
+
+int lgd_sell_set_variant(lgd_sell *h, int variant)
+{
+    return guard([&] {
+        Sell& s = sell_of(h);
+        LGD_REQUIRE(variant >= 0 && variant <= 2, LGD_ERR_INVALID, "SELL kernel variant must lie in [0, 2]");
+        s.variant = variant;
     });
 }
 

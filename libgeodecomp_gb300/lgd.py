@@ -89,6 +89,7 @@ def lib():
             "lgd_gpu_device_ptr": [P, I, I, P, P],
             "lgd_gpu_launch_count": [P, P],
             "lgd_gpu_set_time_block": [P, I],
+            "lgd_gpu_set_variant": [P, I],
             "lgd_gpu_stream": [P, P],
             "lgd_sell_plan": [I, P, I, I, P, P, P, P, P],
             "lgd_sell_fill": [I, P, P, P, I, P, P, ctypes.c_int64, I, P, P],
@@ -102,6 +103,7 @@ def lib():
             "lgd_sell_synchronize": [P],
             "lgd_sell_stream": [P, P],
             "lgd_sell_launch_count": [P, P],
+            "lgd_sell_set_variant": [P, I],
             "lgd_lbm_create": [I, P, P, ctypes.c_double, I, P],
             "lgd_lbm_destroy": [P],
             "lgd_lbm_step": [P, I],
@@ -242,6 +244,10 @@ class Grid:
     def set_time_block(self, depth: int):
         check(lib().lgd_gpu_set_time_block(self._h, depth))
 
+    def set_variant(self, variant: int):
+        """Kernel variant of cells that have several (identical results)."""
+        check(lib().lgd_gpu_set_variant(self._h, variant))
+
     def fixed_point_exponent(self) -> int:
         e = ctypes.c_int()
         check(lib().lgd_gpu_fixed_point_exponent(self._h, ctypes.byref(e)))
@@ -340,6 +346,10 @@ class SellGrid:
         n = ctypes.c_uint64()
         check(lib().lgd_sell_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_variant(self, variant: int):
+        """Kernel variant (identical results): 0 pipelined, 1 unpipelined, 2 pipelined depth 2."""
+        check(lib().lgd_sell_set_variant(self._h, variant))
 
 
 # ------------------------------------------------------------ LBM ensemble

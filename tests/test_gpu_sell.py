@@ -27,11 +27,12 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def gpu_run(n, seed, steps, C=32, sigma=256, precision=8, exact=False):
+def gpu_run(n, seed, steps, C=32, sigma=256, precision=8, exact=False, variant=0):
     rp, col, w = workloads.powerlaw_graph(n, seed=seed)
     x0 = workloads.sell_values(n, seed=seed)
     s = lgd.sell_build(n, rp, col, w, C, sigma)
     with lgd.SellGrid(s, precision=precision, exact=exact) as g:
+        g.set_variant(variant)
         g.upload(x0)
         g.step(steps)
         return g.download(), s, x0
@@ -48,10 +49,40 @@ def test_sell_exact_bit_identical_to_reference():
     np.testing.assert_array_equal(out, g["out"])
 
 
-def test_sell_fused_within_1e12_of_reference():
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_sell_exact_every_kernel_variant_bit_identical(variant):
     g = load("sell_diffusion_2000")
-    out, _, _ = gpu_run(2000, int(g["seed"]), int(g["steps"]))
+    out, _, _ = gpu_run(2000, int(g["seed"]), int(g["steps"]), exact=True, variant=variant)
+    np.testing.assert_array_equal(out, g["out"])
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_sell_fused_within_1e12_of_reference(variant):
+    g = load("sell_diffusion_2000")
+    out, _, _ = gpu_run(2000, int(g["seed"]), int(g["steps"]), variant=variant)
     assert rel_err(out, g["out"]) <= 1e-12
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_sell_ragged_rows_every_variant(variant):
+    # rows of length 0 .. 9 (every residue of the pipeline depth), C = 8
+    rng = np.random.default_rng(5)
+    n = 300
+    deg = rng.integers(0, 10, size=n)
+    rp = np.zeros(n + 1, dtype=np.int64)
+    rp[1:] = np.cumsum(deg)
+    col = rng.integers(0, n, size=int(rp[-1])).astype(np.int32)
+    w = rng.random(int(rp[-1]))
+    x0 = rng.random(n)
+    s = lgd.sell_build(n, rp, col, w, 8, 32)
+    with lgd.SellGrid(s, exact=True) as g:
+        g.set_variant(variant)
+        g.upload(x0)
+        g.step(3)
+        out = g.download()
+    s_ref = oracle.sell_build(n, rp, col, w, 8, 32)
+    ref = oracle.sell_diffusion(s_ref, 8, x0[s_ref["perm"]], 3)
+    np.testing.assert_array_equal(out[s_ref["perm"]], ref)
 
 
 def test_sell_100k_golden():

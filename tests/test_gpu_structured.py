@@ -324,6 +324,43 @@ def test_varcoef_f32_register_kernel_equals_shared_memory_kernel():
         assert np.linalg.norm(r - ref) / np.linalg.norm(ref) < 1e-6
 
 
+@pytest.mark.parametrize("shape,periodic", [((16, 32, 64), 7), ((9, 19, 70), 7), ((20, 17, 130), 0),
+                                            ((7, 33, 66), 1), ((12, 16, 64), 2), ((18, 5, 128), 4),
+                                            ((6, 40, 100), 3), ((3, 2, 2), 7), ((33, 18, 200), 6)])
+def test_varcoef_f64_tma_kernel_equals_register_and_shared_memory_kernels(shape, periodic):
+    """The TMA kernel (variant 6: applies on these grids - zero edges, even
+    rows) against the thread-loaded kernels, bit for bit in FP64, on every
+    mix of wrapping axes and on tiles cut by the grid's edge."""
+    rng = np.random.default_rng(sum(shape) + periodic)
+    u0 = rng.random(shape)
+    k = 0.02 + 0.13 * rng.random(shape)
+    res = []
+    for variant in (6, 1, 2):
+        with lgd.Grid(lgd.CELL_VARCOEF_F64, shape, periodic=periodic) as g:
+            _set_variant(g, variant)
+            g.upload(0, u0)
+            g.upload(1, k)
+            g.step(7)
+            res.append(g.download(0))
+    np.testing.assert_array_equal(res[0], res[1])
+    np.testing.assert_array_equal(res[0], res[2])
+    if periodic == 7:
+        np.testing.assert_array_equal(res[0], oracle.varcoef(u0, k, 7))
+
+
+def test_varcoef_f32_tma_kernel_against_fp64():
+    u0, k = workloads.varcoef_fields(96, seed=11, length=8.0)
+    with lgd.Grid(lgd.CELL_VARCOEF_F32, u0.shape, periodic=7) as g:
+        g.upload(0, u0.astype(np.float32))
+        g.upload(1, k.astype(np.float32))
+        g.step(40)
+        out = g.download(0).astype(np.float64)
+    ref = oracle.varcoef(u0, k, 40)
+    rel_l2 = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    assert rel_l2 < 1e-6, rel_l2
+    assert np.max(np.abs(out - ref)) < 1e-5
+
+
 # ------------------------------------------ kernel variants and fast paths
 def _set_variant(g, v):
     fn = lgd.lib().lgd_gpu_set_variant
