@@ -64,6 +64,11 @@ int lgd_lbm_synchronize(lgd_lbm *h);
 int lgd_lbm_stream(lgd_lbm *h, void **stream);
 int lgd_lbm_launch_count(lgd_lbm *h, uint64_t *count);
 
+/* Memory path of the kernel (identical results): 0 (default) plain loads
+ * and stores; 1 populations read through the read-only data path, results
+ * written with evict-first stores. */
+int lgd_lbm_set_variant(lgd_lbm *h, int variant);
+
 #ifdef __cplusplus
 }
 #endif

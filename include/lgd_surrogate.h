@@ -59,6 +59,15 @@ int lgd_net_synchronize(lgd_net *h);
 int lgd_net_stream(lgd_net *h, void **stream);
 int lgd_net_launch_count(lgd_net *h, uint64_t *count);
 
+/* Inference path: 0 (default) runs the two C -> C layers on the tcgen05
+ * tensor cores (TMA-fed input planes, accumulators in tensor memory) when
+ * the handle has no training buffers, C = 24, nx is a multiple of 128 and
+ * ny even; 1 runs every layer on the mma.sync kernels (the training
+ * path's).  Results agree to BF16 rounding of the activations. */
+int lgd_net_set_variant(lgd_net *h, int variant);
+/* *yes = 1 when forward / advance run the tcgen05 layers. */
+int lgd_net_uses_tensor_core_path(lgd_net *h, int *yes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -453,6 +453,63 @@ static void encode(CUtensorMap *map, void *base, const Grid& g, CUtensorMapDataT
 
 }  // namespace tmak
 
+void encode_tensor_map(void *map, int dtype, int rank, void *base, const uint64_t *dims, const uint64_t *strides,
+                       const uint32_t *box)
+{
+    tmak::EncodeTiledFn fn = tmak::encode_fn();
+    LGD_REQUIRE(fn != nullptr, LGD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    LGD_REQUIRE(rank >= 1 && rank <= 5, LGD_ERR_INVALID, "tensor map rank out of range");
+    cuuint64_t d[5], s[4];
+    cuuint32_t b[5], e[5];
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        e[i] = 1;
+        if (i + 1 < rank) s[i] = strides[i];
+    }
+    CUresult r = fn(reinterpret_cast<CUtensorMap *>(map), (CUtensorMapDataType)dtype, (cuuint32_t)rank, base, d, s, b, e,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    LGD_REQUIRE(r == CUDA_SUCCESS, LGD_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+namespace tmak {
+
+// Planes per CTA of a z-marching launch over xy tiles per plane: the split
+// that minimises the modelled time, waves of resident CTAs times planes per
+// CTA (including the two halo planes), with chunks of at least 8 planes.
+// A partial last wave costs a whole wave: the kernels are bound by the
+// copies each CTA keeps in flight, so fewer CTAs move fewer bytes.
+static int pick_zchunk(long long xy, int nz, long long resident)
+{
+    int best_chunk = nz;
+    double best = 1e300;
+    const int max_split = std::max(1, nz / 8);
+    for (int split = 1; split <= max_split; ++split) {
+        const int chunk = (nz + split - 1) / split;
+        const int s = (nz + chunk - 1) / chunk;
+        const long long waves = (xy * s + resident - 1) / resident;
+        const double t = (double)waves * (chunk + 2);
+        if (t < best * 0.999) {
+            best = t;
+            best_chunk = chunk;
+        }
+    }
+    return best_chunk;
+}
+
+// resident CTAs of a kernel on the whole device
+static long long resident_ctas(const void *fn, int threads, int smem)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    LGD_CHECK_CUDA(cudaGetDevice(&dev));
+    LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    return (long long)sms * std::max(1, per_sm);
+}
+
+}  // namespace tmak
+
 long long fix_edge(const Grid& g);
 
 // The TMA kernel serves Jacobi cells on cube grids whose edge cell is zero
@@ -491,7 +548,11 @@ static void launch_tma_typed(Grid& g, CUtensorMapDataType dt)
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
     const long long xy = (long long)bx * by;
-    // about four waves of four resident CTAs per SM
+    // about 16 CTAs per SM over the launch (several waves of three resident
+    // ones): at 94% of HBM bandwidth the kernel is bound by DRAM, not by
+    // the copies a CTA has in flight, and short z chunks keep the tail of
+    // the launch short (measured: 400 GLUPS at 512^3 against 387 with the
+    // wave-count model the var-coef kernel uses)
     int zsplit = (int)((152LL * 16 + xy - 1) / xy);
     zsplit = std::max(1, std::min(zsplit, (g.desc.nz + 15) / 16));
     int zchunk = (g.desc.nz + zsplit - 1) / zsplit;
@@ -535,19 +596,15 @@ static void launch_varcoef_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.vtmap_base[src][1] = kbuf;
     }
     const int smem = tmak::S * tmak::vc::Lay<R>::SLOT;
-    static bool configured = false;
-    if (!configured) {
+    static long long resident = 0;
+    if (resident == 0) {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::varcoef_tma_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        configured = true;
+        resident = tmak::resident_ctas((const void *)tmak::varcoef_tma_kernel<R>, tmak::THREADS, smem);
     }
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
-    const long long xy = (long long)bx * by;
-    // about four waves of three resident CTAs per SM
-    int zsplit = (int)((152LL * 12 + xy - 1) / xy);
-    zsplit = std::max(1, std::min(zsplit, (g.desc.nz + 15) / 16));
-    int zchunk = (g.desc.nz + zsplit - 1) / zsplit;
-    zsplit = (g.desc.nz + zchunk - 1) / zchunk;
+    const int zchunk = tmak::pick_zchunk((long long)bx * by, g.desc.nz, resident);
+    const int zsplit = (g.desc.nz + zchunk - 1) / zchunk;
     tmak::varcoef_tma_kernel<R><<<dim3(bx, by, zsplit), tmak::THREADS, smem, g.stream>>>(
         *maps, (R *)g.m[0].buf[1 - src], (long)(g.pitch_bytes[0] / sizeof(R)), g.desc.nx, g.desc.ny, g.desc.nz,
         g.desc.periodic, zchunk, g.d_err);

@@ -117,6 +117,12 @@ void launch_jacobi7_tma(Grid& g);
 bool varcoef_tma_applicable(const Grid& g);
 void launch_varcoef_tma(Grid& g);
 
+// cuTensorMapEncodeTiled (tiled, no swizzle, no out-of-bounds NaN fill)
+// into a 128-byte map: dtype a CUtensorMapDataType, dims and box innermost
+// first, strides in bytes for dimensions 1 .. rank-1
+void encode_tensor_map(void *map, int dtype, int rank, void *base, const uint64_t *dims, const uint64_t *strides,
+                       const uint32_t *box);
+
 // kernels, one entry per cell family (implemented in k_*.cu)
 void launch_jacobi7(Grid& g, int steps);
 void launch_gol(Grid& g, int steps);

@@ -66,8 +66,10 @@ struct Geo {
 };
 
 // Halo tile of the layer input for the CTA at (x0, y0, z, b): (TX+2) x 6 x 3
-// voxels, wrapped on the torus, CIN BF16 channels each (CIN even).
-template<int CIN, int TX>
+// voxels, wrapped on the torus, CIN BF16 channels each (CIN even).  GIN:
+// the input is ghosted ([batch][nz+2][ny+2][nx+2][32], the wrapped
+// neighbours stored in the ghost layer), else dense [V][CIN].
+template<int CIN, int TX, bool GIN = false>
 __device__ __forceinline__ void load_halo(uint32_t *halo, const bf16 *__restrict__ in, const Geo& g, int x0, int y0,
                                           int z, int b)
 {
@@ -85,19 +87,52 @@ __device__ __forceinline__ void load_halo(uint32_t *halo, const bf16 *__restrict
         int gx = x0 - 1 + hx;
         int gy = y0 - 1 + hy;
         int gz = z - 1 + hz;
-        gx = (gx < 0) ? gx + g.nx : (gx >= g.nx ? gx - g.nx : gx);
-        gy = (gy < 0) ? gy + g.ny : (gy >= g.ny ? gy - g.ny : gy);
-        gz = (gz < 0) ? gz + g.nz : (gz >= g.nz ? gz - g.nz : gz);
-        const long long v = (((long long)b * g.nz + gz) * g.ny + gy) * g.nx + gx;
-        halo[i] = src[v * WORDS + w];
+        if (GIN) {
+            const long long v = (((long long)b * (g.nz + 2) + gz + 1) * (g.ny + 2) + gy + 1) * (g.nx + 2) + gx + 1;
+            halo[i] = src[v * 16 + w];
+        } else {
+            gx = (gx < 0) ? gx + g.nx : (gx >= g.nx ? gx - g.nx : gx);
+            gy = (gy < 0) ? gy + g.ny : (gy >= g.ny ? gy - g.ny : gy);
+            gz = (gz < 0) ? gz + g.nz : (gz >= g.nz ? gz - g.nz : gz);
+            const long long v = (((long long)b * g.nz + gz) * g.ny + gy) * g.nx + gx;
+            halo[i] = src[v * WORDS + w];
+        }
+    }
+}
+
+// BF16 pair (channels co, co+1) of voxel (x, y, z, b) into a ghosted
+// activation buffer, at its own position and its ghost copies
+__device__ __forceinline__ void store_ghosted(bf16 *__restrict__ out, const Geo& g, int x, int y, int z, int b, int co,
+                                              uint32_t pair)
+{
+    int xs[3], ys[3], zs[3];
+    int nxs = 1, nys = 1, nzs = 1;
+    xs[0] = x + 1;
+    if (x == 0) xs[nxs++] = g.nx + 1;
+    if (x == g.nx - 1) xs[nxs++] = 0;
+    ys[0] = y + 1;
+    if (y == 0) ys[nys++] = g.ny + 1;
+    if (y == g.ny - 1) ys[nys++] = 0;
+    zs[0] = z + 1;
+    if (z == 0) zs[nzs++] = g.nz + 1;
+    if (z == g.nz - 1) zs[nzs++] = 0;
+    for (int a = 0; a < nzs; ++a) {
+        for (int c = 0; c < nys; ++c) {
+            for (int d = 0; d < nxs; ++d) {
+                const long long v = (((long long)b * (g.nz + 2) + zs[a]) * (g.ny + 2) + ys[c]) * (g.nx + 2) + xs[d];
+                *reinterpret_cast<uint32_t *>(out + v * 32 + co) = pair;
+            }
+        }
     }
 }
 
 // ------------------------------------------------------------ forward conv
 // MODE 0: out_h = gelu(acc + bias) in BF16 (COUT even), out_z = acc + bias
 //         in FP32 when non-null.  MODE 1: out_f = acc (+ bias when
-//         non-null) in FP32 for co < COUT.
-template<int CIN, int COUT, int TX, int MODE>
+//         non-null) in FP32 for co < COUT.  MODE 2: as MODE 0 without
+//         out_z, into a ghosted buffer (own position and ghost copies).
+// GIN: the input is ghosted (see load_halo).
+template<int CIN, int COUT, int TX, int MODE, bool GIN = false>
 __global__ void __launch_bounds__(THREADS)
 conv_fwd_kernel(const bf16 *__restrict__ in, const uint2 *__restrict__ wfrag, const float *__restrict__ bias, Geo g,
                 bf16 *__restrict__ out_h, float *__restrict__ out_z, float *__restrict__ out_f)
@@ -116,7 +151,7 @@ conv_fwd_kernel(const bf16 *__restrict__ in, const uint2 *__restrict__ wfrag, co
     const int y0 = blockIdx.y * TYT;
     const int z = blockIdx.z % g.nz;
     const int b = blockIdx.z / g.nz;
-    load_halo<CIN, TX>(halo, in, g, x0, y0, z, b);
+    load_halo<CIN, TX, GIN>(halo, in, g, x0, y0, z, b);
     for (int i = threadIdx.x; i < KS * NT * 32; i += THREADS) wsm[i] = wfrag[i];
     __syncthreads();
 
@@ -187,6 +222,13 @@ conv_fwd_kernel(const bf16 *__restrict__ in, const uint2 *__restrict__ wfrag, co
                         }
                         *reinterpret_cast<uint32_t *>(out_h + v * COUT + co) =
                             pack2(__float2bfloat16(gelu_f(z0)), __float2bfloat16(gelu_f(z1)));
+                    }
+                } else if (MODE == 2) {
+                    if (co < COUT) {
+                        const float z0 = r0 + bias[co];
+                        const float z1 = r1 + bias[co + 1];
+                        store_ghosted(out_h, g, x, y, z, b, co,
+                                      pack2(__float2bfloat16(gelu_f(z0)), __float2bfloat16(gelu_f(z1))));
                     }
                 } else {
                     if (co < COUT) out_f[v * COUT + co] = r0 + (bias ? bias[co] : 0.f);
@@ -455,7 +497,21 @@ struct Net {
     int t;              // Adam step
     cudaStream_t stream;
     uint64_t launches;
+    // tensor-core (tcgen05) inference path: C = 24, nx % 128 == 0, ny even,
+    // no training buffers; layers 2 and 3 on tcgen05, 1 and 4 on mma.sync
+    bool fast;
+    int variant;        // 0: tcgen05 path where it applies; 1: mma.sync for every layer
+    bf16 *hg[2];        // ghosted activations [batch][nz+2][ny+2][nx+2][32]
+    void *wtc[2];       // weights of layers 2 and 3 in the tcgen05 B layout
+    int *d_err;         // bounded waits of the tcgen05 kernel
+    alignas(64) unsigned char tmap[128];
 };
+
+bool tc_applicable(int nx, int ny, int channels);
+size_t tc_weight_bytes();
+void tc_pack_weights(const float *w, void *out, cudaStream_t stream);
+void tc_conv(void *map_cache, const void *in, void *out, const void *wpacked, const float *bias, int nx, int ny, int nz,
+             int batch, cudaStream_t stream, int *d_err);
 
 static int layer_frag_words(int cin, int cout)
 {
@@ -474,18 +530,18 @@ static size_t wgrad_smem()
     return (size_t)(3 * (TYT + 2) * (TX + 2) * CIN / 2) * 4 + (size_t)TYT * TX * ((COUT + 1) & ~1) * 2;
 }
 
-template<int CIN, int COUT, int TX, int MODE>
+template<int CIN, int COUT, int TX, int MODE, bool GIN = false>
 static void run_fwd(Net& n, const bf16 *in, const uint2 *frag, const float *bias, bf16 *oh, float *oz, float *of)
 {
     const size_t sm = fwd_smem<CIN, COUT, TX>();
     static bool configured = false;   // per instantiation, per process
     if (!configured) {
-        LGD_CHECK_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, TX, MODE>,
+        LGD_CHECK_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, TX, MODE, GIN>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         configured = true;
     }
     dim3 grid(n.g.nx / TX, n.g.ny / TYT, n.g.nz * n.g.batch);
-    conv_fwd_kernel<CIN, COUT, TX, MODE><<<grid, THREADS, sm, n.stream>>>(in, frag, bias, n.g, oh, oz, of);
+    conv_fwd_kernel<CIN, COUT, TX, MODE, GIN><<<grid, THREADS, sm, n.stream>>>(in, frag, bias, n.g, oh, oz, of);
     check_launch("conv forward");
     ++n.launches;
 }
@@ -522,6 +578,29 @@ static void repack(Net& n)
         n.launches += 2;
     }
     check_launch("pack fragments");
+    if (n.fast) {
+        tc_pack_weights(n.params + n.L[1].w_off, n.wtc[0], n.stream);
+        tc_pack_weights(n.params + n.L[2].w_off, n.wtc[1], n.stream);
+        n.launches += 2;
+    }
+}
+
+// Inference with the tcgen05 layers: input packing, layer 1 (mma.sync) into
+// a ghosted buffer, layers 2 and 3 on tcgen05 between the two ghosted
+// buffers, layer 4 (mma.sync) from the ghosted buffer into du
+template<int TX>
+static void forward_fast_impl(Net& n, const float *u, const float *k, float *du)
+{
+    pack_input_kernel<<<grid_blocks(n.V), 256, 0, n.stream>>>(u, k, n.x0, n.V);
+    ++n.launches;
+    run_fwd<2, 24, TX, 2>(n, n.x0, n.L[0].frag, n.params + n.L[0].b_off, n.hg[0], nullptr, nullptr);
+    tc_conv(n.tmap, n.hg[0], n.hg[1], n.wtc[0], n.params + n.L[1].b_off, n.g.nx, n.g.ny, n.g.nz, n.g.batch, n.stream,
+            n.d_err);
+    ++n.launches;
+    tc_conv(n.tmap, n.hg[1], n.hg[0], n.wtc[1], n.params + n.L[2].b_off, n.g.nx, n.g.ny, n.g.nz, n.g.batch, n.stream,
+            n.d_err);
+    ++n.launches;
+    run_fwd<24, 1, TX, 1, true>(n, n.hg[0], n.L[3].frag, n.params + n.L[3].b_off, nullptr, nullptr, du);
 }
 
 // the network's channel count is a template parameter of the kernels; the
@@ -578,6 +657,10 @@ static void backward_impl(Net& n, const float *target, double *loss_out)
 
 static void forward(Net& n, const float *u, const float *k, float *du)
 {
+    if (n.fast && n.variant == 0) {
+        if (n.TX == 64) forward_fast_impl<64>(n, u, k, du); else forward_fast_impl<32>(n, u, k, du);
+        return;
+    }
     if (n.C == 24) {
         if (n.TX == 64) forward_impl<24, 64>(n, u, k, du); else forward_impl<24, 32>(n, u, k, du);
     } else {
@@ -615,6 +698,11 @@ static void net_free(Net& n)
     cudaFree(n.dzb);
     cudaFree(n.dz4);
     cudaFree(n.d_loss);
+    cudaFree(n.hg[0]);
+    cudaFree(n.hg[1]);
+    cudaFree(n.wtc[0]);
+    cudaFree(n.wtc[1]);
+    cudaFree(n.d_err);
     if (n.stream) cudaStreamDestroy(n.stream);
 }
 
@@ -706,6 +794,18 @@ int lgd_net_create(int nx, int ny, int nz, int batch, int channels, int training
                 LGD_CHECK_CUDA(cudaMalloc(&n->dzb, sizeof(bf16) * C * V));
                 LGD_CHECK_CUDA(cudaMalloc(&n->dz4, sizeof(bf16) * 2 * V));
                 LGD_CHECK_CUDA(cudaMalloc(&n->d_loss, sizeof(double)));
+            }
+            n->fast = !n->training && tc_applicable(nx, ny, C);
+            if (n->fast) {
+                const size_t gbytes = (size_t)batch * (nz + 2) * (ny + 2) * (nx + 2) * 32 * sizeof(bf16);
+                for (int i = 0; i < 2; ++i) {
+                    LGD_CHECK_CUDA(cudaMalloc(&n->hg[i], gbytes));
+                    // channels 24..31 stay zero (layer 1 writes only 0..23)
+                    LGD_CHECK_CUDA(cudaMemsetAsync(n->hg[i], 0, gbytes, n->stream));
+                    LGD_CHECK_CUDA(cudaMalloc(&n->wtc[i], tc_weight_bytes()));
+                }
+                LGD_CHECK_CUDA(cudaMalloc(&n->d_err, sizeof(int)));
+                LGD_CHECK_CUDA(cudaMemsetAsync(n->d_err, 0, sizeof(int), n->stream));
             }
             repack(*n);
             LGD_CHECK_CUDA(cudaStreamSynchronize(n->stream));
@@ -819,7 +919,36 @@ int lgd_net_advance(lgd_net *h, float *d_u, const float *d_kappa, int calls)
 
 int lgd_net_synchronize(lgd_net *h)
 {
-    return guard([&] { LGD_CHECK_CUDA(cudaStreamSynchronize(net_of(h).stream)); });
+    return guard([&] {
+        Net& n = net_of(h);
+        LGD_CHECK_CUDA(cudaStreamSynchronize(n.stream));
+        if (n.d_err) {
+            int e = 0;
+            LGD_CHECK_CUDA(cudaMemcpy(&e, n.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+            if (e) {
+                LGD_CHECK_CUDA(cudaMemset(n.d_err, 0, sizeof(int)));
+                throw Error(LGD_ERR_TIMEOUT, "tensor-core convolution gave up waiting for its copies or MMAs");
+            }
+        }
+    });
+}
+
+int lgd_net_set_variant(lgd_net *h, int variant)
+{
+    return guard([&] {
+        Net& n = net_of(h);
+        LGD_REQUIRE(variant == 0 || variant == 1, LGD_ERR_INVALID, "network variant must be 0 or 1");
+        n.variant = variant;
+    });
+}
+
+int lgd_net_uses_tensor_core_path(lgd_net *h, int *yes)
+{
+    return guard([&] {
+        LGD_REQUIRE(yes != nullptr, LGD_ERR_INVALID, "null output");
+        Net& n = net_of(h);
+        *yes = (n.fast && n.variant == 0) ? 1 : 0;
+    });
 }
 
 int lgd_net_stream(lgd_net *h, void **stream)

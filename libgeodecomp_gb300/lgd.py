@@ -118,6 +118,7 @@ def lib():
             "lgd_lbm_synchronize": [P],
             "lgd_lbm_stream": [P, P],
             "lgd_lbm_launch_count": [P, P],
+            "lgd_lbm_set_variant": [P, I],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -430,3 +431,7 @@ class LbmEnsemble:
         n = ctypes.c_uint64()
         check(lib().lgd_lbm_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_variant(self, variant: int):
+        """Memory path (identical results): 0 plain, 1 read-only loads + evict-first stores."""
+        check(lib().lgd_lbm_set_variant(self._h, variant))

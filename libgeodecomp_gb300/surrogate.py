@@ -44,6 +44,8 @@ def _bind():
         "lgd_net_synchronize": [P],
         "lgd_net_stream": [P, P],
         "lgd_net_launch_count": [P, P],
+        "lgd_net_set_variant": [P, I],
+        "lgd_net_uses_tensor_core_path": [P, P],
     }.items():
         fn = getattr(L, name)
         fn.argtypes = args
@@ -139,6 +141,16 @@ class SurrogateNet:
         n = ctypes.c_uint64()
         lgd.check(self._L.lgd_net_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_variant(self, variant: int):
+        """0: tcgen05 layers where they apply (inference, C = 24, nx % 128 == 0,
+        ny even); 1: mma.sync for every layer."""
+        lgd.check(self._L.lgd_net_set_variant(self._h, variant))
+
+    def uses_tensor_core_path(self) -> bool:
+        y = ctypes.c_int()
+        lgd.check(self._L.lgd_net_uses_tensor_core_path(self._h, ctypes.byref(y)))
+        return bool(y.value)
 
 
 class PlainStencil:

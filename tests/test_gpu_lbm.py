@@ -60,6 +60,21 @@ def test_lbm_persistent_equals_looped_launches():
             np.testing.assert_array_equal(a.download(j), b.download(j))
 
 
+@pytest.mark.parametrize("precision", [4, 8])
+def test_lbm_memory_path_variants_identical(precision):
+    edges, omegas = workloads.lbm_ensemble(10, seed=9, edge_min=3, edge_max=21)
+    out = []
+    for variant in (0, 1):
+        with lgd.LbmEnsemble(edges, omegas, precision=precision) as e:
+            e.set_variant(variant)
+            e.step(9)
+            out.append([e.download(j) for j in range(len(edges))])
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+    if precision == 8:
+        np.testing.assert_array_equal(out[0][4], oracle.lbm(int(edges[4]), 9, float(omegas[4]), 0.05))
+
+
 def test_lbm_tuner_picks_a_valid_shape_and_reset_restores_rest_state():
     edges, omegas = workloads.lbm_ensemble(16, seed=4, edge_min=8, edge_max=24)
     with lgd.LbmEnsemble(edges, omegas, precision=4) as e:

@@ -43,6 +43,45 @@ def test_forward_matches_fp64_reference(channels, n):
     assert rel < 3e-2, rel   # BF16 activations and weights, FP32 accumulation
 
 
+def _forward_gpu(p, u, k, variant):
+    nz, ny, nx = u.shape
+    with _net((nz, ny, nx), 24) as net:
+        net.set_params(p.astype(np.float32))
+        net.set_variant(variant)
+        used_tc = net.uses_tensor_core_path()
+        ut = torch.tensor(u, dtype=torch.float32, device="cuda").reshape(1, nz, ny, nx)
+        kt = torch.tensor(k, dtype=torch.float32, device="cuda").reshape(1, nz, ny, nx)
+        du = torch.empty_like(ut)
+        net.forward(ut, kt, du)
+        net.synchronize()
+        return du.cpu().numpy().reshape(nz, ny, nx).astype(np.float64), used_tc
+
+
+@pytest.mark.parametrize("shape", [(6, 4, 128), (5, 12, 256), (1, 4, 128)])
+def test_tensor_core_layers_match_fp64_reference_and_mma_sync_path(shape):
+    """Layers 2 and 3 on tcgen05 (ghosted activations, TMA-fed planes, TMEM
+    accumulators): against the FP64 reference within the BF16 tolerance of
+    the mma.sync path, and against the mma.sync path itself; shapes with
+    one plane, two rows and several 128-voxel row tiles exercise the ghost
+    copies on every face."""
+    rng = np.random.default_rng(sum(shape))
+    u = rng.random(shape)
+    k = 0.02 + 0.13 * rng.random(shape)
+    p = sr.init_params(24, seed=8)
+    p[-1] = 0.01
+    ref, _ = sr.forward(p, u, k, 24)
+    tc, used = _forward_gpu(p, u, k, 0)
+    assert used
+    ms, used_ms = _forward_gpu(p, u, k, 1)
+    assert not used_ms
+    scale = np.linalg.norm(ref)
+    assert np.linalg.norm(tc - ref) / scale < 3e-2
+    assert np.linalg.norm(ms - ref) / scale < 3e-2
+    # the two GPU paths round the same FP32 sums to BF16; they differ only
+    # where the summation order flips a rounding
+    assert np.linalg.norm(tc - ms) / scale < 1e-2, np.linalg.norm(tc - ms) / scale
+
+
 def test_gradients_match_fp64_reference():
     channels, n = 8, 32
     u, k, rng = _fields(n, 4)
