@@ -133,22 +133,27 @@ class JacobiWorkload:
     run_steps = 100
     bytes_per_unit = 16          # one FP64 read + one FP64 write per cell and step
 
-    def __init__(self, ieee: bool, edge: int = 512):
+    def __init__(self, ieee: bool, edge: int = 512, f32: bool = False):
         from libgeodecomp_gb300 import lgd, workloads
         self.shape = (edge, edge, edge)
         self.lgd = lgd
         self.ieee = ieee
-        self.name = ("jacobi7_f64_ieee_%d" if ieee else "jacobi7_f64_%d") % edge
+        self.f32 = f32
+        self.name = ("jacobi7_f32_%d" if f32 else "jacobi7_f64_ieee_%d" if ieee else "jacobi7_f64_%d") % edge
         self.metric = JACOBI_METRIC
         self.unit = "GLUPS"
         self.units = int(np.prod(self.shape))
-        self.dtype = "f64" if ieee else "f64 (values on the device in 64-bit fixed point, integer arithmetic)"
-        cell = lgd.CELL_JACOBI7_F64 if ieee else lgd.CELL_JACOBI7_F64_FIX
+        self.dtype = "f32" if f32 else "f64" if ieee else \
+            "f64 (values on the device in 64-bit fixed point, integer arithmetic)"
+        if f32:
+            self.bytes_per_unit = 8
+        cell = lgd.CELL_JACOBI7_F32 if f32 else lgd.CELL_JACOBI7_F64 if ieee else lgd.CELL_JACOBI7_F64_FIX
         self.g = lgd.Grid(cell, self.shape, periodic=0)
         self.g.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
+        self.time_block = 0
         self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "constant 0",
                        "cells": self.units,
-                       "l2": "inputs larger than L2 (%d MiB per buffer)" % (self.units * 8 >> 20),
+                       "l2": "inputs larger than L2 (%d MiB per buffer)" % (self.units * (4 if f32 else 8) >> 20),
                        "cell_update": "(c+n+s+e+w+t+b)*(1/7)"}
 
     def stream(self):
@@ -159,6 +164,16 @@ class JacobiWorkload:
     def step(self, n=1):
         self.g.step(n)
 
+    def set_time_block(self, depth, shape=0):
+        """Steps fused per pass (0 = the library's default for the cell)."""
+        self.g.set_time_block(depth)
+        self.g.set_time_block_shape(shape)
+        self.time_block = depth
+        self.config["time_block"] = "library default" if depth == 0 else depth
+
+    def traffic_key(self):
+        return self.name if self.ieee else "%s_tb%s" % (self.name, self.time_block or "default")
+
     def sync(self):
         self.g.synchronize()
 
@@ -166,9 +181,10 @@ class JacobiWorkload:
         return self.g.launch_count()
 
     def host_buffers(self, torch):
-        nbytes = self.units * 8
-        hin = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64).reshape(self.shape)
-        hout = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64).reshape(self.shape)
+        dt = np.float32 if self.f32 else np.float64
+        nbytes = self.units * np.dtype(dt).itemsize
+        hin = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(self.shape)
+        hout = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(self.shape)
         self.g.download(0, out=hin)
         return hin, hout
 
@@ -382,6 +398,8 @@ def make_workload(name, size=512, lbm_instances=512, lbm_edge_max=192, lbm_tune=
         return JacobiWorkload(ieee=False, edge=size)
     if name == "jacobi7_f64_ieee_512":
         return JacobiWorkload(ieee=True, edge=size)
+    if name == "jacobi7_f32_512":
+        return JacobiWorkload(ieee=False, edge=size, f32=True)
     if name == "gol_u8_8192":
         return GoLWorkload()
     if name == "sell_f64_4m":
@@ -391,12 +409,12 @@ def make_workload(name, size=512, lbm_instances=512, lbm_edge_max=192, lbm_tune=
     raise ValueError(name)
 
 
-WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "gol_u8_8192", "sell_f64_4m", "lbm_d3q19_ensemble_512",
+WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "jacobi7_f32_512", "gol_u8_8192", "sell_f64_4m", "lbm_d3q19_ensemble_512",
                   "varcoef_f32_256"]
 METRICS = {"gol_u8_8192": "Game of Life GLUPS", "sell_f64_4m": "SELL-C-sigma diffusion GB/s and s/step",
            "lbm_d3q19_ensemble_512": "D3Q19 ensemble GLUPS (one persistent launch per step)",
            "varcoef_f32_256": "variable-coefficient diffusion GLUPS"}
-DTYPES = {"gol_u8_8192": "u8", "lbm_d3q19_ensemble_512": "f32", "varcoef_f32_256": "f32"}
+DTYPES = {"gol_u8_8192": "u8", "lbm_d3q19_ensemble_512": "f32", "varcoef_f32_256": "f32", "jacobi7_f32_512": "f32"}
 
 
 # ------------------------------------------------------------------ helpers
@@ -426,12 +444,14 @@ def max_over_ranks(dist, v: float) -> float:
 
 
 def time_steps(torch, w, steps):
+    """CUDA-event time (ms) of `steps` time steps issued as one call, on the
+    library's stream: the library may fuse several steps into one pass
+    (temporal blocking), exactly as a user's lgd_gpu_step(h, 0, steps)."""
     stream = torch.cuda.ExternalStream(w.stream())
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     start.record(stream)
-    for _ in range(steps):
-        w.step(1)
+    w.step(steps)
     end.record(stream)
     end.synchronize()
     return start.elapsed_time(end)
@@ -441,8 +461,9 @@ def run_gpu(args, world, rank, local, dist):
     import torch
     torch.cuda.set_device(local)
     w = make_workload(args.workload, args.size, args.lbm_instances, args.lbm_edge_max, not args.lbm_no_tune)
-    for _ in range(args.warmup):
-        w.step(1)
+    if hasattr(w, "set_time_block"):
+        w.set_time_block(args.time_block, args.time_block_shape)
+    w.step(args.warmup)
     w.sync()
     launches0 = w.launches()
     barrier(dist)
@@ -458,14 +479,21 @@ def run_gpu(args, world, rank, local, dist):
     value = w.units * args.steps * world / (ms * 1e-3) / 1e9
 
     peak, peak_kind = load_peaks()
+    # per launch: one pass over memory, which advances steps_per_launch
+    # time steps (1 without temporal blocking); algorithmic bytes of a pass
+    # are bytes_per_unit per cell (every cell read once and written once)
+    launch_ms = ms / max(1, launches)
     algo_bytes = w.units * w.bytes_per_unit
-    achieved = algo_bytes / (ms_per_step * 1e-3) / 1e9
-    traffic = profile_traffic(w.name)
+    achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
+    traffic = profile_traffic(w.traffic_key() if hasattr(w, "traffic_key") else w.name)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6800 GB/s",
-                "algorithmic_bytes_per_launch": int(algo_bytes), "launch_ms": round(ms_per_step, 4),
-                "traffic": traffic}
+                "algorithmic_bytes_per_launch": int(algo_bytes), "launch_ms": round(launch_ms, 4),
+                "steps_per_launch": round(args.steps / max(1, launches), 3), "traffic": traffic}
+    if launches and launches < args.steps:
+        roofline["effective_gbs_one_step_per_pass"] = round(w.units * w.bytes_per_unit * args.steps / (ms * 1e-3) / 1e9,
+                                                            1)
 
     e2e = None
     if not args.no_e2e and args.workload != "lbm_d3q19_ensemble_512":
@@ -486,6 +514,18 @@ def run_gpu(args, world, rank, local, dist):
 
     extra = {}
     if args.workload == "jacobi7_f64_512" and not args.no_ieee:
+        # the same grid at the other blocking depths (steps fused per pass)
+        sweep = {}
+        for depth in (1, 2, 3, 4):
+            if depth == (args.time_block or 1):
+                continue
+            w.set_time_block(depth)
+            w.step(2 * depth)
+            k = 4 * depth
+            msd = time_steps(torch, w, k) / k
+            sweep[str(depth)] = {"glups": round(w.units / (msd * 1e-3) / 1e9, 2), "ms_per_step": round(msd, 4),
+                                 "hbm_frac_per_pass": round(w.units * 16 / (msd * depth * 1e-3) / 1e9 / peak, 4)}
+        extra["time_block_sweep"] = sweep
         w.close()
         wi = make_workload("jacobi7_f64_ieee_512", args.size)
         for _ in range(3):
@@ -657,6 +697,8 @@ def main():
     ap.add_argument("--workload", choices=WORKLOAD_NAMES, default="jacobi7_f64_512")
     ap.add_argument("--e2e-runs", type=int, default=2)
     ap.add_argument("--size", type=int, default=512, help="cube edge of the Jacobi workloads (small profiling cases)")
+    ap.add_argument("--time-block", type=int, default=0, help="Jacobi steps fused per pass (0 = library default)")
+    ap.add_argument("--time-block-shape", type=int, default=0, help="box shape of the fused passes (tuning)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ieee", action="store_true")

@@ -210,9 +210,25 @@ int lgd_gpu_device_ptr(lgd_handle *h, int member, int which, void **ptr, size_t 
 /* Number of kernel launches this handle has issued (for benchmarking). */
 int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count);
 
-/* Temporal blocking depth used by lgd_gpu_step where the cell supports it
- * (time steps fused per pass over memory); 0 = library default. */
+/* Temporal blocking depth used by lgd_gpu_step (time steps fused into one
+ * pass over memory): 0 = library default (4 for LGD_CELL_JACOBI7_F32, 1 for
+ * the others), 1 = one step per pass, 2 .. LGD_TB_MAX_DEPTH.
+ * Results are bit-identical for every depth.  It applies to the fixed-point
+ * and FP32 Jacobi cells on 3D cube grids with a zero edge cell, under kernel
+ * variants 0 and 6; a count of steps that is not a multiple of the depth
+ * ends with one shorter pass.  Plays the role of the reference's
+ * CacheBlockingSimulator pipelineLength, a wavefront of time steps over
+ * z-marching frames (parallelization/cacheblockingsimulator.h:36-56); the
+ * reference's CUDASimulator runs one step per launch
+ * (parallelization/cudasimulator.h:560-594). */
+#define LGD_TB_MAX_DEPTH 4
 int lgd_gpu_set_time_block(lgd_handle *h, int depth);
+
+/* Box shape of the temporally blocked passes, for tuning and comparison:
+ * 0 = the default for the cell and depth, 1 and 2 = alternatives (warps x
+ * rows per warp; see k_tb.cu); a shape that does not exist for a depth runs
+ * the default.  Results do not depend on the shape. */
+int lgd_gpu_set_time_block_shape(lgd_handle *h, int shape);
 
 #ifdef __cplusplus
 }

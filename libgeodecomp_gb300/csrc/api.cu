@@ -627,8 +627,17 @@ int lgd_gpu_set_time_block(lgd_handle *h, int depth)
 {
     return guard([&] {
         Grid& g = grid_of(h);
-        LGD_REQUIRE(depth >= 0 && depth <= 64, LGD_ERR_INVALID, "time block depth out of range");
+        LGD_REQUIRE(depth >= 0 && depth <= LGD_TB_MAX_DEPTH, LGD_ERR_INVALID, "time block depth out of range");
         g.time_block = depth;
+    });
+}
+
+int lgd_gpu_set_time_block_shape(lgd_handle *h, int shape)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(shape >= 0 && shape <= 2, LGD_ERR_INVALID, "time block shape must lie in [0, 2]");
+        g.tb_shape = shape;
     });
 }
 

@@ -500,6 +500,16 @@ static void launch_zcol(Grid& g, View<const typename CELL::T> in, View<typename 
 void launch_jacobi7(Grid& g, int steps)
 {
     if ((g.variant == 0 || g.variant == 6) && tma_applicable(g)) {
+        // temporal blocking: passes of `depth` steps, then one shorter pass
+        // for the remainder (single steps go through the one-step kernel)
+        const int depth = (g.time_block == 0) ? (tb_applicable(g) ? tb_default_depth(g) : 1) : g.time_block;
+        if (depth > 1 && tb_applicable(g)) {
+            while (steps >= 2) {
+                const int d = steps >= depth ? depth : steps;
+                launch_jacobi7_tb(g, d, g.tb_shape);
+                steps -= d;
+            }
+        }
         for (int s = 0; s < steps; ++s) launch_jacobi7_tma(g);
         return;
     }

@@ -24,6 +24,7 @@
 
 #include "lgd_internal.h"
 #include "k_cells.cuh"
+#include "k_tma.cuh"
 
 namespace lgd {
 namespace tmak {
@@ -34,7 +35,6 @@ constexpr int ROWS = 4;
 constexpr int THREADS = 128;
 constexpr int D = 3;           // prefetch distance in planes
 constexpr int S = D + 2;       // ring slots: planes q-1, q, q+1 in use, D ahead
-constexpr long long WAIT_CYCLES = 4000000000LL;
 
 template<typename T>
 struct Box {
@@ -44,68 +44,6 @@ struct Box {
     static constexpr int BYTES = W * H * (int)sizeof(T);
     static constexpr int SLOT = (BYTES + 127) / 128 * 128;
 };
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n"
-        " .reg .pred p;\n"
-        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n"
-        "}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > WAIT_CYCLES) return false;
-    }
-    return true;
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
-
-template<typename T>
-__device__ __forceinline__ void lds_pair(const unsigned char *p, T& a, T& b)
-{
-    if (sizeof(T) == 8) {
-        const longlong2 v = *reinterpret_cast<const longlong2 *>(p);
-        a = *reinterpret_cast<const T *>(&v.x);
-        b = *reinterpret_cast<const T *>(&v.y);
-    } else {
-        const int2 v = *reinterpret_cast<const int2 *>(p);
-        a = *reinterpret_cast<const T *>(&v.x);
-        b = *reinterpret_cast<const T *>(&v.y);
-    }
-}
 
 template<typename CELL>
 __global__ void __launch_bounds__(THREADS)

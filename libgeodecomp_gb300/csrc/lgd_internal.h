@@ -86,6 +86,7 @@ struct Grid {
     size_t plane_elems;     // pitch_elems * ny
     int cur;                // index of the current buffer
     int time_block;         // temporal blocking depth (0 = default)
+    int tb_shape;           // temporal blocking box shape (0 = default for the cell and depth)
     int fix_exp;            // fixed-point grids: value = k * 2^(fix_exp - LGD_FIX_BITS)
     int variant;            // kernel variant where a cell has several (0 = default)
     cudaStream_t stream;
@@ -110,12 +111,21 @@ struct Grid {
     alignas(64) unsigned char vtmap[2][6 * 128];
     bool vtmap_ready[2];
     void *vtmap_base[2][2];
+    // temporal-blocking kernel: one tensor map per buffer (box 64 x rows)
+    alignas(64) unsigned char tbmap[2][128];
+    bool tbmap_ready[2];
+    void *tbmap_base[2];
+    int tbmap_rows[2];
 };
 
 bool tma_applicable(const Grid& g);
 void launch_jacobi7_tma(Grid& g);
 bool varcoef_tma_applicable(const Grid& g);
 void launch_varcoef_tma(Grid& g);
+// temporal blocking (k_tb.cu): depth time steps per pass, 2 .. LGD_TB_MAX_DEPTH
+bool tb_applicable(const Grid& g);
+int tb_default_depth(const Grid& g);
+void launch_jacobi7_tb(Grid& g, int depth, int shape);
 
 // cuTensorMapEncodeTiled (tiled, no swizzle, no out-of-bounds NaN fill)
 // into a 128-byte map: dtype a CUtensorMapDataType, dims and box innermost

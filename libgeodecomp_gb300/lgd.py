@@ -20,6 +20,7 @@ ERR_CUDA = 3
 ERR_NOMEM = 4
 ERR_TIMEOUT = 5
 ERR_UNSUPPORTED = 6
+TB_MAX_DEPTH = 4        # LGD_TB_MAX_DEPTH
 
 CELL_JACOBI7_F64 = 1
 CELL_JACOBI7_F64_FIX = 2
@@ -89,6 +90,7 @@ def lib():
             "lgd_gpu_device_ptr": [P, I, I, P, P],
             "lgd_gpu_launch_count": [P, P],
             "lgd_gpu_set_time_block": [P, I],
+            "lgd_gpu_set_time_block_shape": [P, I],
             "lgd_gpu_set_variant": [P, I],
             "lgd_gpu_stream": [P, P],
             "lgd_sell_plan": [I, P, I, I, P, P, P, P, P],
@@ -244,6 +246,9 @@ class Grid:
 
     def set_time_block(self, depth: int):
         check(lib().lgd_gpu_set_time_block(self._h, depth))
+
+    def set_time_block_shape(self, shape: int):
+        check(lib().lgd_gpu_set_time_block_shape(self._h, shape))
 
     def set_variant(self, variant: int):
         """Kernel variant of cells that have several (identical results)."""

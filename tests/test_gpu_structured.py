@@ -427,3 +427,99 @@ def test_jacobi7_tma_kernel_equals_register_kernel(shape, cell):
             g.step(7)
             res.append(g.download(0))
     np.testing.assert_array_equal(res[0], res[1])
+
+
+# ------------------------------------------------------ temporal blocking
+TB_SHAPES = [(9, 20, 128), (70, 16, 64), (33, 61, 130), (5, 40, 70), (2, 1, 37), (1, 8, 192), (40, 33, 65),
+             (3, 17, 1), (12, 70, 250)]
+
+
+def _run_blocked(cell, u0, steps, depth, shape=0):
+    with lgd.Grid(cell, u0.shape) as g:
+        g.set_time_block(depth)
+        g.set_time_block_shape(shape)
+        g.upload(0, u0)
+        before = g.launch_count()
+        g.step(steps)
+        passes = g.launch_count() - before
+        return g.download(0), passes
+
+
+def _passes(steps, depth):
+    """Launches of `steps` steps at blocking depth `depth`: full passes, one
+    shorter pass for a remainder of two or more, a single step otherwise."""
+    if depth <= 1:
+        return steps
+    full, rem = divmod(steps, depth)
+    return full + (1 if rem >= 2 else rem)
+
+
+@pytest.mark.parametrize("grid_shape", TB_SHAPES)
+@pytest.mark.parametrize("cell", [lgd.CELL_JACOBI7_F64_FIX, lgd.CELL_JACOBI7_F32])
+@pytest.mark.parametrize("depth", [2, 3, 4])
+def test_temporal_blocking_bit_identical_to_single_steps(grid_shape, cell, depth):
+    """depth steps per pass over memory (intermediate levels on chip) give
+    exactly the single-step results: ragged tiles in x and y, z chunks,
+    degenerate axes, a step count that leaves a remainder pass."""
+    u0 = workloads.jacobi_initial(grid_shape[2], grid_shape[1], grid_shape[0], seed=23)
+    if cell == lgd.CELL_JACOBI7_F32:
+        u0 = u0.astype(np.float32)
+    steps = 2 * depth + 1 + (depth > 2)
+    ref, n_ref = _run_blocked(cell, u0, steps, 1)
+    assert n_ref == steps
+    out, n = _run_blocked(cell, u0, steps, depth)
+    assert n == _passes(steps, depth)
+    np.testing.assert_array_equal(out, ref)
+
+
+@pytest.mark.parametrize("cell,depth,shape", [(lgd.CELL_JACOBI7_F64_FIX, 2, 1), (lgd.CELL_JACOBI7_F64_FIX, 2, 2),
+                                              (lgd.CELL_JACOBI7_F64_FIX, 3, 1), (lgd.CELL_JACOBI7_F64_FIX, 4, 1),
+                                              (lgd.CELL_JACOBI7_F32, 4, 1), (lgd.CELL_JACOBI7_F32, 4, 2)])
+@pytest.mark.parametrize("grid_shape", [(33, 61, 130), (70, 16, 64), (2, 1, 37), (12, 70, 250)])
+def test_temporal_blocking_box_shapes(cell, depth, shape, grid_shape):
+    u0 = workloads.jacobi_initial(grid_shape[2], grid_shape[1], grid_shape[0], seed=29)
+    if cell == lgd.CELL_JACOBI7_F32:
+        u0 = u0.astype(np.float32)
+    steps = 3 * depth
+    ref, _ = _run_blocked(cell, u0, steps, 1)
+    out, n = _run_blocked(cell, u0, steps, depth, shape)
+    assert n == 3
+    np.testing.assert_array_equal(out, ref)
+
+
+def test_temporal_blocking_fixed_point_128_config_within_1e12():
+    """The Jacobi configuration (128^3, 100 steps) at every blocking depth:
+    within 1e-12 of the reference's FP64 result, identical across depths."""
+    g = load("jacobi7_cube_128")
+    u0 = workloads.jacobi_initial(128, 128, 128, seed=42)
+    ref = oracle.jacobi7(u0, 100)
+    assert sha(ref) == str(g["sha256"])
+    outs = [_run_blocked(lgd.CELL_JACOBI7_F64_FIX, u0, 100, d)[0] for d in (1, 2, 3, 4)]
+    for o in outs:
+        assert rel_err(o, ref) <= 1e-12
+        np.testing.assert_array_equal(o, outs[0])
+
+
+def test_temporal_blocking_default_depth_and_limits():
+    u0 = workloads.jacobi_initial(64, 32, 16, seed=3)
+    with lgd.Grid(lgd.CELL_JACOBI7_F32, u0.shape) as g:
+        g.upload(0, u0.astype(np.float32))
+        before = g.launch_count()
+        g.step(10)
+        assert g.launch_count() - before == 3          # FP32 default depth 4: 4 + 4 + 2
+    with lgd.Grid(lgd.CELL_JACOBI7_F64_FIX, u0.shape) as g:
+        g.upload(0, u0)
+        before = g.launch_count()
+        g.step(10)
+        assert g.launch_count() - before == 10         # fixed point default: one step per pass
+        with pytest.raises(lgd.LGDError):
+            g.set_time_block(lgd.TB_MAX_DEPTH + 1)
+        with pytest.raises(lgd.LGDError):
+            g.set_time_block_shape(3)
+    with lgd.Grid(lgd.CELL_JACOBI7_F64, u0.shape) as g:     # IEEE FP64: one step per pass
+        g.set_time_block(4)
+        g.upload(0, u0)
+        before = g.launch_count()
+        g.step(8)
+        assert g.launch_count() - before == 8
+        np.testing.assert_array_equal(g.download(0), oracle.jacobi7(u0, 8))
