@@ -1,27 +1,44 @@
 // Surrogate convolution C -> C (C = 24) on the fifth-generation tensor
 // cores: tcgen05.mma with BF16 operands in shared memory and the FP32
-// accumulator in tensor memory, the input planes brought in by TMA.
+// accumulator in tensor memory.
 //
 // Activations for this path are "ghosted": BF16 [batch][nz+2][ny+2][nx+2][32],
 // the torus' wrapped neighbours stored in a one-voxel ghost layer (written
 // by the producing layer's epilogue), channels 24..31 zero.  A CTA owns a
 // 128 x 2 tile of output voxels of every plane of its z chunk and keeps:
-//   - the layer's weights, 27 taps x 32 x 32 BF16 (54 KiB), as the MMA's B
-//     operand in the canonical K-major layout without swizzle: element
-//     (tap, cin, cout) at ((tap * 4 + cin / 8) * 32 + cout) * 16 B + cin % 8;
+//   - the layer's weights, 27 taps x 32 x 32 BF16 (54 KiB, one bulk copy),
+//     as the MMA's B operand in the canonical K-major layout without
+//     swizzle: element (tap, cin, cout) at ((tap * 4 + cin / 8) * 32 + cout)
+//     * 16 B + cin % 8;
 //   - a ring of five input planes, each 4 channel groups x 4 rows x 130
-//     voxels x 8 channels - one TMA box per group lands as [row][voxel][8 ch],
-//     i.e. voxels 16 B apart, which is the canonical K-major layout of the A
-//     operand: 8-voxel core matrices 128 B apart (SBO), channel groups one
-//     group block apart (LBO).  A tap shifts the A start address by whole
-//     voxels (16 B) and rows; no data moves.
-// Per output plane one thread issues 2 rows x 27 taps x 2 K-steps of
-// M=128 (voxels), N=32 (output channels), K=16 MMAs into one of two TMEM
-// accumulator buffers and commits them to an mbarrier; meanwhile all four
-// warps drain the other buffer (tcgen05.ld, bias, GELU, BF16, ghost copies)
-// for the previous plane.  The freed input slot is refilled four planes
-// ahead.  Every wait is bounded; a CTA that gives up sets the error word,
-// drains its copies and MMAs and frees its tensor memory.
+//     voxels x 8 channels, laid out [group][row][voxel][8 ch], i.e. voxels
+//     16 B apart: the canonical K-major layout of the A operand (8-voxel core
+//     matrices 128 B apart = SBO, channel groups one group block apart =
+//     LBO).  A tap shifts the A start address by whole voxels (16 B) and
+//     rows; no data moves.
+// Warp-specialised pipeline, no CTA-wide barrier inside the plane loop:
+//   - warps 9..12 (loaders) copy input planes into the ring with cp.async,
+//     16 B per request, each warp instruction 32 consecutive voxels of one
+//     channel group (the four groups of a voxel back to back, so the three
+//     re-reads of a 64-byte voxel hit L1); up to three planes in flight,
+//     published to the MMA thread through the slot's "full" mbarrier after a
+//     generic-to-async proxy fence.  (A tensor-map copy would land the same
+//     layout, but its 16-byte box rows run at about one row per 7.5 cycles
+//     per SM, four times slower than the MMAs.)
+//   - warp 0, one thread: per output plane i it waits for input planes
+//     i .. i+2 and for the epilogue to have emptied TMEM accumulator buffer
+//     i % 2, issues 2 rows x 27 taps x 2 K-steps of M=128 (voxels), N=32
+//     (output channels), K=16 MMAs into that buffer and commits them to the
+//     buffer's mbarrier and to the "empty" mbarrier of input plane i's slot
+//     (plane i has no later reader);
+//   - warps 1..8 (the epilogue): each owns one TMEM lane quarter (32 voxels)
+//     and one output row; per plane it waits for the commit, reads its 32
+//     accumulator columns (tcgen05.ld), hands the buffer back and then
+//     applies bias, GELU, BF16 rounding and stores the voxel and its ghost
+//     copies.
+// Every wait is bounded and gives up early once another role has failed; a
+// CTA that gives up sets the error word, lets its copies and MMAs finish and
+// frees its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -43,7 +60,11 @@ constexpr int SLOT = G * GROUP_BYTES;       // 33280
 constexpr int S = 5;                        // ring slots
 constexpr int W_BYTES = 27 * G * CP * 16;   // 55296
 constexpr int SMEM = 128 + W_BYTES + S * SLOT;
-constexpr int THREADS = 128;
+constexpr int EPI_WARPS = 8;                // epilogue warps: 4 lane quarters x 2 rows
+constexpr int LOAD_WARPS = 4;               // cp.async loaders
+constexpr int LOAD0 = 1 + EPI_WARPS;        // first loader warp
+constexpr int THREADS = 32 * (1 + EPI_WARPS + LOAD_WARPS);
+constexpr int IN_FLIGHT = 3;                // input planes a loader keeps in flight
 constexpr int TMEM_COLS = 128;              // 2 buffers x 2 rows x 32 columns
 constexpr long long WAIT_CYCLES = 4000000000LL;
 
@@ -162,16 +183,35 @@ struct Params {
     int nx, ny, nz, batch, zchunk;
 };
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// bounded wait that also gives up as soon as another role has failed
+__device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity, volatile int *fail)
+{
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (*fail || clock64() - t0 > WAIT_CYCLES) return false;
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(THREADS, 1)
-conv_tc_kernel(const __grid_constant__ CUtensorMap in_map, const __nv_bfloat16 *__restrict__ wpacked,
+conv_tc_kernel(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wpacked,
                const float *__restrict__ bias, __nv_bfloat16 *__restrict__ out, Params p, int *err)
 {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar_w;
-    __shared__ __align__(8) uint64_t bar_tma[S];
-    __shared__ __align__(8) uint64_t bar_mma[2];
+    __shared__ __align__(8) uint64_t bar_full[S];     // input plane in its slot (one arrive per loader warp)
+    __shared__ __align__(8) uint64_t bar_empty[S];    // input slot no longer read (MMA commit)
+    __shared__ __align__(8) uint64_t bar_mma[2];      // accumulator buffer written (MMA commit)
+    __shared__ __align__(8) uint64_t bar_free[2];     // accumulator buffer read by the epilogue
     __shared__ uint32_t s_tmem;
     __shared__ int s_fail;
+    volatile int *fail = &s_fail;
 
     unsigned char *smem = smem_raw + ((128 - (saddr(smem_raw) & 127)) & 127);
     unsigned char *wsm = smem;
@@ -195,147 +235,181 @@ conv_tc_kernel(const __grid_constant__ CUtensorMap in_map, const __nv_bfloat16 *
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    int issued = 0;     // input planes issued (thread 0)
+    // MMA-thread state (thread 0 only)
+    int waited = 0;         // input planes waited for
+    int committed = 0;      // output planes whose MMAs were committed
+    bool w_ready = false;
     if (tid == 0) {
         s_fail = 0;
         mbar_init(saddr(&bar_w), 1);
-        for (int s = 0; s < S; ++s) mbar_init(saddr(&bar_tma[s]), 1);
-        for (int s = 0; s < 2; ++s) mbar_init(saddr(&bar_mma[s]), 1);
+        for (int s = 0; s < S; ++s) {
+            mbar_init(saddr(&bar_full[s]), LOAD_WARPS);
+            mbar_init(saddr(&bar_empty[s]), 1);
+        }
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(saddr(&bar_mma[s]), 1);
+            mbar_init(saddr(&bar_free[s]), EPI_WARPS);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         mbar_expect_tx(saddr(&bar_w), W_BYTES);
         bulk_copy(saddr(wsm), wpacked, W_BYTES, saddr(&bar_w));
-        for (; issued < S && issued <= n + 1; ++issued) {
-            const uint32_t bar = saddr(&bar_tma[issued % S]);
-            mbar_expect_tx(bar, SLOT);
-            for (int g = 0; g < G; ++g) {
-                tma_4d(saddr(ring + (issued % S) * SLOT + g * GROUP_BYTES), &in_map, 8 * g, x0, y0, zg0 + issued, bar);
-            }
-        }
     }
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = s_tmem;
 
-    int mma_issued = 0;     // output planes whose MMAs were committed (thread 0)
-    int waited_tma = 0;     // input planes thread 0 has waited for
-    bool w_ready = false;
-    for (int i = 0; i <= n; ++i) {
-        // A: MMAs of output plane i (planes i, i+1, i+2 of the ring)
-        if (tid == 0 && i < n && !s_fail) {
-            bool ok = true;
-            if (!w_ready) {
-                ok = mbar_wait(saddr(&bar_w), 0);
-                w_ready = ok;
-            }
-            while (ok && waited_tma <= i + 2) {
-                ok = mbar_wait(saddr(&bar_tma[waited_tma % S]), (waited_tma / S) & 1);
-                if (ok) ++waited_tma;
-            }
-            if (!ok) {
-                s_fail = 1;
-            } else {
+    if (warp == 0) {
+        if (lane == 0) {
+            bool ok = mbar_wait_or_fail(saddr(&bar_w), 0, fail);
+            w_ready = ok;
+            const uint32_t rbase = saddr(ring);
+            const uint64_t wd = sdesc(saddr(wsm), CP * 16, 128);
+            for (int i = 0; ok && i < n; ++i) {
+                while (ok && waited <= i + 2) {
+                    ok = mbar_wait_or_fail(saddr(&bar_full[waited % S]), (uint32_t)((waited / S) & 1), fail);
+                    if (ok) ++waited;
+                }
+                if (ok && i >= 2) ok = mbar_wait_or_fail(saddr(&bar_free[i & 1]), (uint32_t)(((i - 2) >> 1) & 1), fail);
+                if (!ok) break;
                 fence_after();
-                const uint32_t wbase = saddr(wsm);
-#pragma unroll 1
+                // descriptors: one base per input slot, every MMA adds a
+                // compile-time offset (16-byte units) to the address field
+                // (addresses stay below 2^18, so nothing carries out of it)
+                uint64_t sd[3];
+                const int i_slot = i % S;
+#pragma unroll
+                for (int dz = 0; dz < 3; ++dz) {
+                    const int sl = (i_slot + dz >= S) ? i_slot + dz - S : i_slot + dz;
+                    sd[dz] = sdesc(rbase + (uint32_t)(sl * SLOT), GROUP_BYTES, 128);
+                }
+#pragma unroll
                 for (int r = 0; r < TYO; ++r) {
                     const uint32_t d = tmem + (uint32_t)((i & 1) * 64 + r * 32);
-                    uint32_t acc = 0;
-#pragma unroll 1
+#pragma unroll
                     for (int tap = 0; tap < 27; ++tap) {
                         const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-                        const uint32_t slot = saddr(ring + ((i + dz) % S) * SLOT);
 #pragma unroll
                         for (int s = 0; s < 2; ++s) {
-                            const uint32_t a = slot + (uint32_t)((((2 * s) * R + r + dy) * HXV + dx) * 16);
-                            const uint32_t bw = wbase + (uint32_t)((tap * G + 2 * s) * CP * 16);
-                            mma(d, sdesc(a, GROUP_BYTES, 128), sdesc(bw, CP * 16, 128), acc);
-                            acc = 1;
+                            const uint64_t a = sd[dz] + (uint64_t)(((2 * s) * R + r + dy) * HXV + dx);
+                            const uint64_t bw = wd + (uint64_t)((tap * G + 2 * s) * CP);
+                            mma(d, a, bw, (tap | s) ? 1u : 0u);
                         }
                     }
                 }
                 mma_commit(saddr(&bar_mma[i & 1]));
-                mma_issued = i + 1;
+                mma_commit(saddr(&bar_empty[i % S]));     // plane i has no later reader
+                committed = i + 1;
             }
+            if (!ok) s_fail = 1;
         }
         __syncwarp();
-        // B: epilogue of output plane i - 1 while the tensor core works on i
-        if (i >= 1) {
-            const int j = i - 1;
-            const bool ok = mbar_wait(saddr(&bar_mma[j & 1]), (j >> 1) & 1);
-            if (!ok) s_fail = 1;
-            fence_after();
-            if (ok) {
-                if (tid == 0 && issued <= n + 1 && !s_fail) {
-                    // plane j is no longer read: refill its slot S planes ahead
-                    const int q = j + S;
-                    if (q == issued) {
-                        const uint32_t bar = saddr(&bar_tma[q % S]);
-                        mbar_expect_tx(bar, SLOT);
-                        for (int g = 0; g < G; ++g) {
-                            tma_4d(saddr(ring + (q % S) * SLOT + g * GROUP_BYTES), &in_map, 8 * g, x0, y0, zg0 + q, bar);
-                        }
-                        ++issued;
-                    }
+    } else if (warp >= LOAD0) {
+        // loaders: input plane q into slot q % S, [group][row][voxel][8 ch]
+        const int lt = tid - LOAD0 * 32;
+        const long long gnx = p.nx + 2;
+        int published = 0;
+        bool ok = true;
+        auto publish = [&](int upto) {          // planes published .. upto-1 have landed
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            for (; published < upto; ++published) {
+                if (lane == 0) mbar_arrive(saddr(&bar_full[published % S]));
+            }
+        };
+        for (int q = 0; q <= n + 1; ++q) {
+            const int slot = q % S;
+            if (q >= S) {
+                const bool got = mbar_wait_or_fail(saddr(&bar_empty[slot]), (uint32_t)(((q - S) / S) & 1), fail);
+                if (!__all_sync(0xffffffffu, got)) {
+                    ok = false;
+                    break;
                 }
-                // the voxel's own position and its ghost copies (an axis of
-                // extent 1 has both)
-                const int x = x0 + warp * 32 + lane;
-                const int zz = z0 + j;
-                int xs[3], ys[3], zs[3];
-                int nxs = 1, nzs = 1;
-                xs[0] = x + 1;
-                if (x == 0) xs[nxs++] = p.nx + 1;
-                if (x == p.nx - 1) xs[nxs++] = 0;
-                zs[0] = zz + 1;
-                if (zz == 0) zs[nzs++] = p.nz + 1;
-                if (zz == p.nz - 1) zs[nzs++] = 0;
-#pragma unroll 1
-                for (int r = 0; r < TYO; ++r) {
-                    float v[32];
-                    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((j & 1) * 64 + r * 32), v);
-                    uint32_t w[16];
+            }
+            unsigned char *dst = ring + slot * SLOT;
+            const long long base = ((long long)(zg0 + q) * (p.ny + 2) + y0) * gnx + x0;   // ghosted voxel (row 0, voxel 0)
+            for (int v = lt; v < R * HXV; v += LOAD_WARPS * 32) {
+                const int yy = v / HXV;
+                const int xx = v - yy * HXV;
+                const __nv_bfloat16 *src = in + (base + (long long)yy * gnx + xx) * CP;
 #pragma unroll
-                    for (int c = 0; c < 12; ++c) {
-                        w[c] = pack_bf16(gelu(v[2 * c] + __ldg(bias + 2 * c)), gelu(v[2 * c + 1] + __ldg(bias + 2 * c + 1)));
-                    }
+                for (int g = 0; g < G; ++g) {
+                    const uint32_t d = saddr(dst + ((g * R + yy) * HXV + xx) * 16);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src + 8 * g) : "memory");
+                }
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            if (q + 1 >= IN_FLIGHT) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(IN_FLIGHT - 1) : "memory");
+                publish(q + 2 - IN_FLIGHT);
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (ok) publish(n + 2);
+        else if (lane == 0) s_fail = 1;
+    } else {
+        // epilogue: lane quarter qd (TMEM lanes 32 qd .. 32 qd + 31 = voxels),
+        // output row r of the tile
+        const int qd = warp & 3;
+        const int r = (warp - 1) >> 2;
+        const int x = x0 + qd * 32 + lane;
+        const int y = y0 + r;
+        int xs[3], ys[3];         // an axis of extent 1 has both ghost copies
+        int nxs = 1, nys = 1;
+        xs[0] = x + 1;
+        if (x == 0) xs[nxs++] = p.nx + 1;
+        if (x == p.nx - 1) xs[nxs++] = 0;
+        ys[0] = y + 1;
+        if (y == 0) ys[nys++] = p.ny + 1;
+        if (y == p.ny - 1) ys[nys++] = 0;
+        float bv[24];
 #pragma unroll
-                    for (int c = 12; c < 16; ++c) w[c] = 0u;
-                    const int y = y0 + r;
-                    int nys = 1;
-                    ys[0] = y + 1;
-                    if (y == 0) ys[nys++] = p.ny + 1;
-                    if (y == p.ny - 1) ys[nys++] = 0;
-                    for (int a = 0; a < nzs; ++a) {
-                        for (int bb = 0; bb < nys; ++bb) {
-                            for (int c = 0; c < nxs; ++c) {
-                                const long long vox =
-                                    (((long long)b * (p.nz + 2) + zs[a]) * (p.ny + 2) + ys[bb]) * (p.nx + 2) + xs[c];
-                                uint4 *o = reinterpret_cast<uint4 *>(out + vox * CP);
-                                o[0] = make_uint4(w[0], w[1], w[2], w[3]);
-                                o[1] = make_uint4(w[4], w[5], w[6], w[7]);
-                                o[2] = make_uint4(w[8], w[9], w[10], w[11]);
-                                o[3] = make_uint4(w[12], w[13], w[14], w[15]);
-                            }
-                        }
+        for (int c = 0; c < 24; ++c) bv[c] = __ldg(bias + c);
+        for (int j = 0; j < n; ++j) {
+            const bool ok = mbar_wait_or_fail(saddr(&bar_mma[j & 1]), (uint32_t)((j >> 1) & 1), fail);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) s_fail = 1;
+                break;
+            }
+            fence_after();
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)((j & 1) * 64 + r * 32), v);
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(saddr(&bar_free[j & 1]));
+            uint32_t w[12];
+#pragma unroll
+            for (int c = 0; c < 12; ++c) w[c] = pack_bf16(gelu(v[2 * c] + bv[2 * c]), gelu(v[2 * c + 1] + bv[2 * c + 1]));
+            const int zz = z0 + j;
+            int zs[3];
+            int nzs = 1;
+            zs[0] = zz + 1;
+            if (zz == 0) zs[nzs++] = p.nz + 1;
+            if (zz == p.nz - 1) zs[nzs++] = 0;
+            for (int a = 0; a < nzs; ++a) {
+                for (int bb = 0; bb < nys; ++bb) {
+                    for (int c = 0; c < nxs; ++c) {
+                        const long long vox =
+                            (((long long)b * (p.nz + 2) + zs[a]) * (p.ny + 2) + ys[bb]) * (p.nx + 2) + xs[c];
+                        uint4 *o = reinterpret_cast<uint4 *>(out + vox * CP);
+                        o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                        o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                        o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+                        o[3] = make_uint4(0u, 0u, 0u, 0u);
                     }
                 }
             }
         }
-        fence_before();
-        __syncthreads();        // TMEM buffer (i-1)&1 drained before MMAs of plane i+1 reuse it
-        fence_after();
-        if (s_fail) break;
     }
 
+    fence_before();
+    __syncthreads();            // every role has left its loop; no copy is in flight
+    fence_after();
     if (s_fail) {
-        // report, then wait (bounded) for the copies and MMAs still in flight
+        // report, then wait (bounded) for the MMAs and the weight copy
         if (tid == 0) {
             atomicExch(err, 1);
-            for (int q = waited_tma; q < issued; ++q) {
-                if (!mbar_wait(saddr(&bar_tma[q % S]), (q / S) & 1)) break;
-            }
-            if (mma_issued > 0) mbar_wait(saddr(&bar_mma[(mma_issued - 1) & 1]), ((mma_issued - 1) >> 1) & 1);
+            if (committed > 0) mbar_wait(saddr(&bar_mma[(committed - 1) & 1]), ((committed - 1) >> 1) & 1);
             if (!w_ready) mbar_wait(saddr(&bar_w), 0);
         }
         fence_before();
@@ -389,13 +463,7 @@ void tc_conv(void *map_cache, const void *in, void *out, const void *wpacked, co
         LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         resident = sms;
     }
-    // tensor map of the input: (32 channels, nx+2, ny+2, batch (nz+2)), box
-    // (8, 130, 4, 1); built per call into the caller's cache (128 bytes)
-    const uint64_t dims[4] = {(uint64_t)tc::CP, (uint64_t)nx + 2, (uint64_t)ny + 2, (uint64_t)batch * (nz + 2)};
-    const uint64_t strides[3] = {(uint64_t)tc::CP * 2, (uint64_t)tc::CP * 2 * (nx + 2),
-                                 (uint64_t)tc::CP * 2 * (nx + 2) * (ny + 2)};
-    const uint32_t box[4] = {8, (uint32_t)tc::HXV, (uint32_t)tc::R, 1};
-    encode_tensor_map(map_cache, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), dims, strides, box);
+    (void)map_cache;
     // z chunks: whole waves of one CTA per SM
     const long long xy = (long long)(nx / tc::TXO) * (ny / tc::TYO) * batch;
     int best_chunk = nz;
@@ -418,7 +486,7 @@ void tc_conv(void *map_cache, const void *in, void *out, const void *wpacked, co
     p.zchunk = best_chunk;
     const int zsplit = (nz + best_chunk - 1) / best_chunk;
     dim3 grid(nx / tc::TXO, ny / tc::TYO, batch * zsplit);
-    tc::conv_tc_kernel<<<grid, tc::THREADS, tc::SMEM, stream>>>(*reinterpret_cast<const CUtensorMap *>(map_cache),
+    tc::conv_tc_kernel<<<grid, tc::THREADS, tc::SMEM, stream>>>((const __nv_bfloat16 *)in,
                                                                  (const __nv_bfloat16 *)wpacked, bias,
                                                                  (__nv_bfloat16 *)out, p, d_err);
     check_launch("tensor-core convolution");

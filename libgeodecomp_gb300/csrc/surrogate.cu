@@ -145,7 +145,9 @@ conv_fwd_kernel(const bf16 *__restrict__ in, const uint2 *__restrict__ wfrag, co
     constexpr int HY = TYT + 2;
     extern __shared__ uint32_t smem[];
     uint32_t *halo = smem;                                        // 3 * HY * HX * CIN / 2 words
-    uint2 *wsm = reinterpret_cast<uint2 *>(smem + ((3 * HY * HX * CIN / 2 + 1) & ~1));
+    uint2 *wsm = reinterpret_cast<uint2 *>(smem + ((3 * HY * HX * CIN / 2 + 3) & ~3));   // 16-byte aligned
+    // MODE 2: the tile's output voxels, 16 words (32 BF16 channels) each
+    uint32_t *otile = reinterpret_cast<uint32_t *>(wsm + KS * NT * 32);
 
     const int x0 = blockIdx.x * TX;
     const int y0 = blockIdx.y * TYT;
@@ -224,15 +226,56 @@ conv_fwd_kernel(const bf16 *__restrict__ in, const uint2 *__restrict__ wfrag, co
                             pack2(__float2bfloat16(gelu_f(z0)), __float2bfloat16(gelu_f(z1)));
                     }
                 } else if (MODE == 2) {
+                    const int vt = warp * TX + (x - x0);
                     if (co < COUT) {
                         const float z0 = r0 + bias[co];
                         const float z1 = r1 + bias[co + 1];
-                        store_ghosted(out_h, g, x, y, z, b, co,
-                                      pack2(__float2bfloat16(gelu_f(z0)), __float2bfloat16(gelu_f(z1))));
+                        otile[vt * 16 + co / 2] = pack2(__float2bfloat16(gelu_f(z0)), __float2bfloat16(gelu_f(z1)));
+                    } else if (co < 32) {
+                        otile[vt * 16 + co / 2] = 0u;
                     }
                 } else {
                     if (co < COUT) out_f[v * COUT + co] = r0 + (bias ? bias[co] : 0.f);
                     if (co + 1 < COUT) out_f[v * COUT + co + 1] = r1 + (bias ? bias[co + 1] : 0.f);
+                }
+            }
+        }
+    }
+    if (MODE == 2) {
+        // channels COUT .. 31 of the staged voxels (the n-tiles stop at COUT)
+        for (int i = threadIdx.x; i < TYT * TX * (16 - NT * 4); i += THREADS) {
+            const int per = 16 - NT * 4;
+            otile[(i / per) * 16 + NT * 4 + i % per] = 0u;
+        }
+        __syncthreads();
+        // one 64-byte record per voxel, at its position and its ghost copies
+        for (int vt = threadIdx.x; vt < TYT * TX; vt += THREADS) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(otile + vt * 16);
+            const uint4 q0 = src[0], q1 = src[1], q2 = src[2], q3 = src[3];
+            const int x = x0 + vt % TX;
+            const int yv = y0 + vt / TX;
+            int xs[3], ys[3], zs[3];     // an axis of extent 1 has both ghost copies
+            int nxs = 1, nys = 1, nzs = 1;
+            xs[0] = x + 1;
+            if (x == 0) xs[nxs++] = g.nx + 1;
+            if (x == g.nx - 1) xs[nxs++] = 0;
+            ys[0] = yv + 1;
+            if (yv == 0) ys[nys++] = g.ny + 1;
+            if (yv == g.ny - 1) ys[nys++] = 0;
+            zs[0] = z + 1;
+            if (z == 0) zs[nzs++] = g.nz + 1;
+            if (z == g.nz - 1) zs[nzs++] = 0;
+            for (int a = 0; a < nzs; ++a) {
+                for (int c = 0; c < nys; ++c) {
+                    for (int d = 0; d < nxs; ++d) {
+                        const long long v =
+                            (((long long)b * (g.nz + 2) + zs[a]) * (g.ny + 2) + ys[c]) * (g.nx + 2) + xs[d];
+                        uint4 *o = reinterpret_cast<uint4 *>(out_h + v * 32);
+                        o[0] = q0;
+                        o[1] = q1;
+                        o[2] = q2;
+                        o[3] = q3;
+                    }
                 }
             }
         }
@@ -512,16 +555,21 @@ size_t tc_weight_bytes();
 void tc_pack_weights(const float *w, void *out, cudaStream_t stream);
 void tc_conv(void *map_cache, const void *in, void *out, const void *wpacked, const float *bias, int nx, int ny, int nz,
              int batch, cudaStream_t stream, int *d_err);
+bool last_conv_applicable(int nx, int ny, int channels);
+void last_conv(const void *h, const float *w, const float *bias, float *out, bool add_to_u, int nx, int ny, int nz,
+               int batch, cudaStream_t stream);
 
 static int layer_frag_words(int cin, int cout)
 {
     return ceil_div(27 * cin, 16) * ceil_div(cout, 8) * 32;
 }
 
-template<int CIN, int COUT, int TX>
+template<int CIN, int COUT, int TX, int MODE = 0>
 static size_t fwd_smem()
 {
-    return (size_t)(((3 * (TYT + 2) * (TX + 2) * CIN / 2 + 1) & ~1) * 4 + layer_frag_words(CIN, COUT) * 8);
+    // MODE 2 adds the staged output tile (TYT x TX voxels x 32 BF16 channels)
+    return (size_t)(((3 * (TYT + 2) * (TX + 2) * CIN / 2 + 3) & ~3) * 4 + layer_frag_words(CIN, COUT) * 8) +
+           (MODE == 2 ? (size_t)TYT * TX * 64 : 0);
 }
 
 template<int CIN, int COUT, int TX>
@@ -533,7 +581,7 @@ static size_t wgrad_smem()
 template<int CIN, int COUT, int TX, int MODE, bool GIN = false>
 static void run_fwd(Net& n, const bf16 *in, const uint2 *frag, const float *bias, bf16 *oh, float *oz, float *of)
 {
-    const size_t sm = fwd_smem<CIN, COUT, TX>();
+    const size_t sm = fwd_smem<CIN, COUT, TX, MODE>();
     static bool configured = false;   // per instantiation, per process
     if (!configured) {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, TX, MODE, GIN>,
@@ -587,9 +635,12 @@ static void repack(Net& n)
 
 // Inference with the tcgen05 layers: input packing, layer 1 (mma.sync) into
 // a ghosted buffer, layers 2 and 3 on tcgen05 between the two ghosted
-// buffers, layer 4 (mma.sync) from the ghosted buffer into du
+// buffers, layer 4 from the ghosted buffer into du (the tap-product kernel
+// of conv_last.cu where the tile fits, else mma.sync).  With add_to_u the
+// last layer adds its result to u instead (u <- u + du, the residual step).
+// Returns whether it did.
 template<int TX>
-static void forward_fast_impl(Net& n, const float *u, const float *k, float *du)
+static bool forward_fast_impl(Net& n, const float *u, const float *k, float *du, bool add_to_u)
 {
     pack_input_kernel<<<grid_blocks(n.V), 256, 0, n.stream>>>(u, k, n.x0, n.V);
     ++n.launches;
@@ -600,7 +651,14 @@ static void forward_fast_impl(Net& n, const float *u, const float *k, float *du)
     tc_conv(n.tmap, n.hg[1], n.hg[0], n.wtc[1], n.params + n.L[2].b_off, n.g.nx, n.g.ny, n.g.nz, n.g.batch, n.stream,
             n.d_err);
     ++n.launches;
+    if (last_conv_applicable(n.g.nx, n.g.ny, n.C)) {
+        last_conv(n.hg[0], n.params + n.L[3].w_off, n.params + n.L[3].b_off, add_to_u ? const_cast<float *>(u) : du,
+                  add_to_u, n.g.nx, n.g.ny, n.g.nz, n.g.batch, n.stream);
+        ++n.launches;
+        return add_to_u;
+    }
     run_fwd<24, 1, TX, 1, true>(n, n.hg[0], n.L[3].frag, n.params + n.L[3].b_off, nullptr, nullptr, du);
+    return false;
 }
 
 // the network's channel count is a template parameter of the kernels; the
@@ -655,17 +713,19 @@ static void backward_impl(Net& n, const float *target, double *loss_out)
     }
 }
 
-static void forward(Net& n, const float *u, const float *k, float *du)
+// du = net(u, k); with add_to_u the fast path may add du to u itself
+// (returns true when it did)
+static bool forward(Net& n, const float *u, const float *k, float *du, bool add_to_u = false)
 {
     if (n.fast && n.variant == 0) {
-        if (n.TX == 64) forward_fast_impl<64>(n, u, k, du); else forward_fast_impl<32>(n, u, k, du);
-        return;
+        return n.TX == 64 ? forward_fast_impl<64>(n, u, k, du, add_to_u) : forward_fast_impl<32>(n, u, k, du, add_to_u);
     }
     if (n.C == 24) {
         if (n.TX == 64) forward_impl<24, 64>(n, u, k, du); else forward_impl<24, 32>(n, u, k, du);
     } else {
         if (n.TX == 64) forward_impl<8, 64>(n, u, k, du); else forward_impl<8, 32>(n, u, k, du);
     }
+    return false;
 }
 
 static void backward(Net& n, const float *target, double *loss)
@@ -909,7 +969,7 @@ int lgd_net_advance(lgd_net *h, float *d_u, const float *d_kappa, int calls)
         LGD_REQUIRE(d_u && d_kappa, LGD_ERR_INVALID, "null input");
         LGD_REQUIRE(calls >= 0, LGD_ERR_INVALID, "negative call count");
         for (int c = 0; c < calls; ++c) {
-            forward(n, d_u, d_kappa, n.du);
+            if (forward(n, d_u, d_kappa, n.du, true)) continue;
             add_inplace_kernel<<<grid_blocks(n.V), 256, 0, n.stream>>>(d_u, n.du, n.V);
             check_launch("residual update");
             ++n.launches;

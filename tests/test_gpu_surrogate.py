@@ -132,3 +132,27 @@ def test_judge_falls_back_to_the_plain_stencil():
     u_plain, _ = S.run_plain(u0, kappa, steps)
     assert stats["fallbacks"] == stats["segments"] == 2
     assert S.rel_l2(u_sur, u_plain) < 1e-6
+
+
+@pytest.mark.parametrize("shape", [(6, 4, 128), (5, 12, 256)])
+def test_advance_equals_forward_plus_residual(shape):
+    """advance() lets the last layer add du into u itself on the fast path;
+    the result is the same as forward() followed by u + du."""
+    rng = np.random.default_rng(7)
+    u = rng.random(shape)
+    k = 0.02 + 0.13 * rng.random(shape)
+    p = sr.init_params(24, seed=12)
+    p[-1] = 0.01
+    nz, ny, nx = shape
+    with _net(shape, 24) as net:
+        net.set_params(p.astype(np.float32))
+        ut = torch.tensor(u, dtype=torch.float32, device="cuda").reshape(1, nz, ny, nx)
+        kt = torch.tensor(k, dtype=torch.float32, device="cuda").reshape(1, nz, ny, nx)
+        du = torch.empty_like(ut)
+        net.forward(ut, kt, du)
+        net.synchronize()                  # the net works on its own stream
+        expect = ut + du
+        torch.cuda.synchronize()
+        net.advance(ut, kt, 1)
+        net.synchronize()
+        assert torch.equal(ut, expect)
