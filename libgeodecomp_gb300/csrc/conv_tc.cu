@@ -20,9 +20,10 @@
 //   - warps 9..12 (loaders) copy input planes into the ring with cp.async,
 //     16 B per request, each warp instruction 32 consecutive voxels of one
 //     channel group (the four groups of a voxel back to back, so the three
-//     re-reads of a 64-byte voxel hit L1); up to three planes in flight,
-//     published to the MMA thread through the slot's "full" mbarrier after a
-//     generic-to-async proxy fence.  (A tensor-map copy would land the same
+//     re-reads of a 64-byte voxel hit L1); two planes in flight, each
+//     published to the MMA thread through the slot's "full" mbarrier (after
+//     a generic-to-async proxy fence) before the loader waits for the next
+//     free slot.  (A tensor-map copy would land the same
 //     layout, but its 16-byte box rows run at about one row per 7.5 cycles
 //     per SM, four times slower than the MMAs.)
 //   - warp 0, one thread: per output plane i it waits for input planes
@@ -64,7 +65,6 @@ constexpr int EPI_WARPS = 8;                // epilogue warps: 4 lane quarters x
 constexpr int LOAD_WARPS = 4;               // cp.async loaders
 constexpr int LOAD0 = 1 + EPI_WARPS;        // first loader warp
 constexpr int THREADS = 32 * (1 + EPI_WARPS + LOAD_WARPS);
-constexpr int IN_FLIGHT = 3;                // input planes a loader keeps in flight
 constexpr int TMEM_COLS = 128;              // 2 buffers x 2 rows x 32 columns
 constexpr long long WAIT_CYCLES = 4000000000LL;
 
@@ -319,6 +319,13 @@ conv_tc_kernel(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__rest
         };
         for (int q = 0; q <= n + 1; ++q) {
             const int slot = q % S;
+            // publish what has landed before waiting for a slot: plane q-2
+            // (all groups but the newest are complete), so the MMAs of the
+            // plane that frees this slot never wait on this loader
+            if (q >= 2) {
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+                publish(q - 1);
+            }
             if (q >= S) {
                 const bool got = mbar_wait_or_fail(saddr(&bar_empty[slot]), (uint32_t)(((q - S) / S) & 1), fail);
                 if (!__all_sync(0xffffffffu, got)) {
@@ -339,10 +346,6 @@ conv_tc_kernel(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__rest
                 }
             }
             asm volatile("cp.async.commit_group;" ::: "memory");
-            if (q + 1 >= IN_FLIGHT) {
-                asm volatile("cp.async.wait_group %0;" ::"n"(IN_FLIGHT - 1) : "memory");
-                publish(q + 2 - IN_FLIGHT);
-            }
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
         if (ok) publish(n + 2);
