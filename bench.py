@@ -172,7 +172,11 @@ class JacobiWorkload:
         self.config["time_block"] = "library default" if depth == 0 else depth
 
     def traffic_key(self):
-        return self.name if self.ieee else "%s_tb%s" % (self.name, self.time_block or "default")
+        """Key of the committed ncu traffic line: the workload, plus _tb<d>
+        when d > 1 steps are fused per pass (the library's default depth is
+        4 for the FP32 cell, 1 for the others)."""
+        depth = self.time_block or (4 if self.f32 else 1)
+        return self.name if depth <= 1 else "%s_tb%d" % (self.name, depth)
 
     def sync(self):
         self.g.synchronize()
@@ -683,6 +687,10 @@ def run_surrogate(args):
     S.run_plain(u0, kap, 16)                         # warm-up
     u_plain, t_plain = S.run_plain(u0, kap, steps)
     u_sur, t_sur, stats = S.run_surrogate_with_judge(params, u0, kap, steps, tol=args.judge_tol)
+    # the same run with a judge that accepts the network's own error level:
+    # what the surrogate path costs and how far it drifts when it is used
+    u_rel, t_rel, st_rel = S.run_surrogate_with_judge(params, u0, kap, steps, tol=args.relaxed_tol)
+    net_ms = S.time_calls(params, u0, kap, calls=8)
     line = {
         "metric": "surrogate vs plain time at rel-L2<=1e-3", "value": round(t_plain / t_sur, 4),
         "unit": "x (plain FP32 stencil time / surrogate-plus-judge time)", "higher_is_better": True,
@@ -696,11 +704,34 @@ def run_surrogate(args):
         "rel_l2_vs_fp64": {"plain_fp32": S.rel_l2(u_plain, u64), "surrogate_judge": S.rel_l2(u_sur, u64)},
         "judge": {"segments": stats["segments"], "fallbacks": stats["fallbacks"],
                   "max_error": max(stats["judge_errors"]) if stats["judge_errors"] else None},
+        "relaxed_judge": {"tol": args.relaxed_tol, "surrogate_judge_s": round(t_rel, 4),
+                          "plain_over_surrogate": round(t_plain / t_rel, 4), "fallbacks": st_rel["fallbacks"],
+                          "segments": st_rel["segments"], "rel_l2_vs_fp64": S.rel_l2(u_rel, u64)},
+        "net_call_ms": round(net_ms, 4),
+        "net_call_tflops": round(S.FLOP_PER_VOXEL * n ** 3 / (net_ms * 1e-3) / 1e12, 1),
+        "plain_16_steps_ms": round(t_plain / steps * S.STEPS_PER_CALL * 1e3, 4),
         "training": {"data_s": round(t_data, 2), "train_s": round(t_train, 2), "loss_first": hist[0],
                      "loss_last": float(np.mean(hist[-20:])),
                      "one_call_rel_l2": {"net": float(err_net), "no_learning_baseline": float(err_id)}},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_net_calls(args):
+    """The surrogate network alone: --net-calls calls (u <- u + net(u, k)) on
+    a --surrogate-size^3 grid with randomly initialised parameters, after
+    one warm-up call (inference path; for profiling the layers)."""
+    import torch
+    from libgeodecomp_gb300 import surrogate as S
+    from libgeodecomp_gb300 import workloads
+    n = args.surrogate_size
+    u0_np, k_np = workloads.varcoef_fields(n, seed=42, length=16.0)
+    u0 = torch.tensor(u0_np, dtype=torch.float32, device="cuda").contiguous()
+    kap = torch.tensor(k_np, dtype=torch.float32, device="cuda").contiguous()
+    ms = S.time_calls(S.init_params(24, seed=0), u0, kap, calls=args.net_calls)
+    print(json.dumps({"metric": "surrogate network call", "value": round(ms, 4), "unit": "ms per call",
+                      "higher_is_better": False, "tflops": round(S.FLOP_PER_VOXEL * n ** 3 / (ms * 1e-3) / 1e12, 1),
+                      "config": {"workload": "surrogate_net_%d" % n, "calls": args.net_calls}}), flush=True)
 
 
 def main():
@@ -725,11 +756,16 @@ def main():
     ap.add_argument("--surrogate-size", type=int, default=256)
     ap.add_argument("--surrogate-steps", type=int, default=4096)
     ap.add_argument("--trajectories", type=int, default=2000)
-    ap.add_argument("--train-iters", type=int, default=1500)
+    ap.add_argument("--train-iters", type=int, default=6000)
     ap.add_argument("--judge-tol", type=float, default=1e-4)
+    ap.add_argument("--relaxed-tol", type=float, default=1e-2)
+    ap.add_argument("--net-calls", type=int, default=0, help="time this many surrogate network calls alone")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.net_calls > 0:
+        run_net_calls(args)
+        return
     if args.surrogate:
         run_surrogate(args)
         return

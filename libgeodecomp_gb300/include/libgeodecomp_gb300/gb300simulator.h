@@ -19,7 +19,10 @@
 //     changes reach the device (the reference leaves this as a fixme,
 //     :450-454);
 //   - blockSize is accepted for signature compatibility and validated; the
-//     library picks its own launch shapes.
+//     library picks its own launch shapes;
+//   - run() hands the steps between two plugin calls to the library in one
+//     call (which may fuse them into fewer passes over memory); the plugin
+//     calls themselves are unchanged.
 //
 // Cells are bound to a kernel compiled into the library by specialising
 // GB300CellTraits<CELL> (see below); the cell class and its API traits stay
@@ -41,6 +44,7 @@
 #include "compat.h"
 #endif
 
+#include <algorithm>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -155,6 +159,7 @@ public:
         handleOutput(WRITER_INITIALIZED);
         while (this->stepNum < this->initializer->maxSteps()) {
             if (feedback.simulationEnded()) break;
+            advanceQuietSteps();
             step(&feedback);
         }
         handleInput(STEERER_ALL_DONE, &feedback);
@@ -239,6 +244,32 @@ private:
             hostGrid->set(*c, cell);
         }
         hostStale = false;
+    }
+
+    // Steps before the next one that calls a plugin: no Steerer runs before
+    // them (stepNum % period != 0), no Writer after them (step % period !=
+    // 0) and none of them is the last.  Those steps go to the library in
+    // one call, which may fuse several of them into one pass over memory
+    // (temporal blocking); the plugins see exactly the calls that
+    // step-by-step execution makes.  Cells with several nano steps keep one
+    // call per step.
+    void advanceQuietSteps()
+    {
+        if (NANO_STEPS != 1) return;
+        const unsigned s = this->stepNum;
+        unsigned next = this->initializer->maxSteps() - 1;     // the last step announces ALL_DONE
+        for (std::size_t i = 0; i < this->steerers.size(); ++i) {
+            const unsigned p = this->steerers[i]->getPeriod();
+            next = std::min(next, (s + p - 1) / p * p);                // stepNum % p == 0
+        }
+        for (std::size_t i = 0; i < this->writers.size(); ++i) {
+            const unsigned p = this->writers[i]->getPeriod();
+            next = std::min(next, (s + 1 + p - 1) / p * p - 1);        // (stepNum + 1) % p == 0
+        }
+        if (next <= s) return;
+        gb300Check(lgd_gpu_step(handle, 0, (int)std::min<unsigned>(next - s, 1u << 30)));
+        this->stepNum = next;
+        hostStale = true;
     }
 
     void handleInput(SteererEvent event, SteererFeedback *feedback)

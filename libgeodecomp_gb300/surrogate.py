@@ -24,6 +24,8 @@ from . import lgd, workloads
 
 STEPS_PER_CALL = 16
 CALLS_PER_JUDGE = 8
+# multiply-adds x 2 per voxel and call: 27 taps x (2x24 + 24x24 + 24x24 + 24x1)
+FLOP_PER_VOXEL = 2 * 27 * (2 * 24 + 24 * 24 + 24 * 24 + 24 * 1)
 
 
 def _bind():
@@ -349,3 +351,27 @@ def run_surrogate_with_judge(params, u0, kappa, steps: int, tol: float = 1e-4, c
     finally:
         net.close()
         plain.close()
+
+
+def time_calls(params, u0, kappa, calls: int = 8, channels: int = 24) -> float:
+    """Milliseconds per network call (u <- u + net(u, kappa)), CUDA events on
+    the network's stream, after one warm-up call."""
+    import torch
+    n = u0.shape[-1]
+    net = SurrogateNet((n, n, n), batch=1, channels=channels)
+    try:
+        net.set_params(params)
+        u = u0.clone()
+        torch.cuda.synchronize()
+        net.advance(u, kappa, 1)
+        net.synchronize()
+        st = torch.cuda.ExternalStream(net.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        net.advance(u, kappa, calls)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / calls
+    finally:
+        net.close()
