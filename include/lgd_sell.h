@@ -58,6 +58,29 @@ int lgd_sell_create(int n, int C, int64_t total, const int32_t *chunk_offset, co
                     lgd_sell **out);
 int lgd_sell_destroy(lgd_sell *h);
 
+/* Builds the SELL-C-sigma matrix on the GPU from a CSR matrix (row_ptr[n+1],
+ * col and w [row_ptr[n]]) and returns a ready handle: the arrays of
+ * lgd_sell_plan + lgd_sell_fill with remap_columns = 1, byte for byte, and
+ * the permutation kept for logical-order copies.  device_input = 0: the CSR
+ * arrays are host memory (copied in); 1: device memory.  Device-path limits:
+ * sigma <= LGD_SELL_GPU_MAX_SIGMA and at most LGD_SELL_GPU_MAX_ROW entries per
+ * row (LGD_ERR_UNSUPPORTED beyond; the host builder has no limit).  Replaces
+ * ReorderingUnstructuredGrid::setWeights with InitFromMatrix
+ * (storage/reorderingunstructuredgrid.h:195-284,
+ * storage/sellcsigmasparsematrixcontainer.h:82-161), which the reference runs
+ * on one host thread. */
+#define LGD_SELL_GPU_MAX_SIGMA 4096
+#define LGD_SELL_GPU_MAX_ROW 1024
+int lgd_sell_create_from_csr(int n, const int64_t *row_ptr, const int32_t *col, const double *w, int C, int sigma,
+                             int device_input, int precision, int flags, lgd_sell **out);
+
+/* Copies a handle's matrix back to host arrays (each pointer may be NULL):
+ * chunk_offset[n_chunks+1], row_length[rows_padded], values[total] (as FP64),
+ * column[total], perm[n] (only if the handle has one); *total gets the slot
+ * count.  For checking and for writers that save the matrix. */
+int lgd_sell_get_layout(lgd_sell *h, int32_t *chunk_offset, int32_t *row_length, double *values, int32_t *column,
+                        int32_t *perm, int64_t *total);
+
 /* Node values (n doubles), current (which = 0) or next (1) buffer;
  * logical = 1 maps through perm (GridBase::get/set on a reordering grid,
  * storage/reorderingunstructuredgrid.h:300-340), 0 uses physical order. */

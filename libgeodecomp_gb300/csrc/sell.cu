@@ -265,6 +265,180 @@ static void launch_sell(Sell& s, int row_begin, int row_end)
     ++s.launches;
 }
 
+
+// ------------------------------------------------------- builder on the GPU
+// The same layout as lgd_sell_plan + lgd_sell_fill, built by kernels:
+//   1. row lengths from row_ptr (checked: non-decreasing, at most
+//      LGD_SELL_GPU_MAX_ROW);
+//   2. per sigma-window a stable sort by decreasing length: one CTA sorts
+//      the keys ((MAX_ROW - length) << 12 | index in window) with a bitonic
+//      network in shared memory - unique keys, so the order is the stable
+//      one of the host's counting sort;
+//   3. row_length[p] = length of perm[p], the inverse permutation;
+//   4. chunk lengths, then one CTA scans C * chunk length into chunk_offset;
+//   5. one warp per physical row ranks the row's entries by (physical
+//      column, position) - the host's stable insertion sort - and writes
+//      value and column to chunk_offset[p / C] + rank * C + p % C.
+// Errors (bad row_ptr, a column outside the node set, a row too long, more
+// than 2^31-1 slots) set bits of a device word that the host checks.
+namespace sbuild {
+
+constexpr int SORT_THREADS = 512;
+constexpr int KEY_BITS = 12;                 // index inside a window: sigma <= 4096
+
+enum { E_ROWPTR = 1, E_LONGROW = 2, E_COLUMN = 4, E_TOTAL = 8 };
+
+__global__ void lengths_kernel(const int64_t *__restrict__ row_ptr, int n, int *__restrict__ len, int *err)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const long long d = row_ptr[r + 1] - row_ptr[r];
+        if (d < 0 || (r == 0 && row_ptr[0] != 0)) {
+            atomicOr(err, E_ROWPTR);
+            len[r] = 0;
+        } else if (d > LGD_SELL_GPU_MAX_ROW) {
+            atomicOr(err, E_LONGROW);
+            len[r] = 0;
+        } else {
+            len[r] = (int)d;
+        }
+    }
+}
+
+// one CTA per window [w0, w0 + cnt); P = the window padded to a power of two
+__global__ void __launch_bounds__(SORT_THREADS)
+window_sort_kernel(const int *__restrict__ len, int n, int sigma, int P, int *__restrict__ perm)
+{
+    extern __shared__ uint32_t keys[];
+    const int w0 = blockIdx.x * sigma;
+    const int cnt = min(sigma, n - w0);
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        keys[i] = (i < cnt) ? ((uint32_t)(LGD_SELL_GPU_MAX_ROW - len[w0 + i]) << KEY_BITS) | (uint32_t)i : 0xffffffffu;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t a = keys[i], b = keys[l];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        perm[w0 + i] = w0 + (int)(keys[i] & ((1u << KEY_BITS) - 1));
+    }
+}
+
+__global__ void row_length_kernel(const int *__restrict__ len, const int *__restrict__ perm, int n, int rows_padded,
+                                  int *__restrict__ row_length, int *__restrict__ inv)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < rows_padded; p += gridDim.x * blockDim.x) {
+        if (p < n) {
+            const int r = perm[p];
+            row_length[p] = len[r];
+            inv[r] = p;
+        } else {
+            row_length[p] = 0;
+        }
+    }
+}
+
+// chunk_offset[c] = sum of C * max row length over the chunks before c, one
+// CTA of 1024 threads, each scanning a contiguous run of chunks
+__global__ void __launch_bounds__(1024)
+chunk_scan_kernel(const int *__restrict__ row_length, int C, int n_chunks, int *__restrict__ chunk_offset,
+                  long long *total, int *err)
+{
+    __shared__ long long part[1024];
+    const int t = threadIdx.x;
+    const int per = (n_chunks + 1023) / 1024;
+    const int c0 = min(n_chunks, t * per);
+    const int c1 = min(n_chunks, c0 + per);
+    long long sum = 0;
+    for (int c = c0; c < c1; ++c) {
+        int m = 0;
+        for (int l = 0; l < C; ++l) m = max(m, row_length[c * C + l]);
+        sum += (long long)m * C;
+    }
+    part[t] = sum;
+    __syncthreads();
+    if (t == 0) {
+        long long acc = 0;
+        for (int i = 0; i < 1024; ++i) {
+            const long long v = part[i];
+            part[i] = acc;
+            acc += v;
+        }
+        *total = acc;
+        if (acc > 0x7fffffffLL) atomicOr(err, E_TOTAL);
+        chunk_offset[n_chunks] = (int)min(acc, 0x7fffffffLL);
+    }
+    __syncthreads();
+    long long acc = part[t];
+    for (int c = c0; c < c1; ++c) {
+        chunk_offset[c] = (int)min(acc, 0x7fffffffLL);
+        int m = 0;
+        for (int l = 0; l < C; ++l) m = max(m, row_length[c * C + l]);
+        acc += (long long)m * C;
+    }
+}
+
+// one warp per physical row: rank the row's entries by (physical column,
+// position) and place them
+template<typename R>
+__global__ void __launch_bounds__(256)
+fill_kernel(const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const double *__restrict__ w,
+            const int *__restrict__ perm, const int *__restrict__ inv, const int *__restrict__ chunk_offset, int n,
+            int C, long long total, R *__restrict__ values, int *__restrict__ column, int *err)
+{
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long p = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < n; p += warps) {
+        const int r = perm[p];
+        const long long b = row_ptr[r];
+        const long long dl = row_ptr[r + 1] - b;
+        const int d = (int)(dl < LGD_SELL_GPU_MAX_ROW ? dl : LGD_SELL_GPU_MAX_ROW);
+        const long long base = (long long)chunk_offset[p / C] + p % C;
+        const int tiles = (d + 31) / 32;
+        // key of entry e: physical column in the high word, position low
+        auto key_of = [&](int e) -> unsigned long long {
+            if (e >= d) return ~0ull;
+            const int c = col[b + e];
+            const int pc = (c >= 0 && c < n) ? inv[c] : 0;
+            return ((unsigned long long)(unsigned)pc << 32) | (unsigned)e;
+        };
+        for (int a = 0; a < tiles; ++a) {
+            const int e = a * 32 + lane;
+            const unsigned long long ke = key_of(e);
+            int rank = 0;
+            for (int t = 0; t < tiles; ++t) {
+                const unsigned long long kt = key_of(t * 32 + lane);
+#pragma unroll 8
+                for (int sft = 0; sft < 32; ++sft) {
+                    rank += (__shfl_sync(0xffffffffu, kt, sft) < ke) ? 1 : 0;
+                }
+            }
+            if (e < d) {
+                const int c = col[b + e];
+                if (c < 0 || c >= n) atomicOr(err, E_COLUMN);
+                const long long slot = base + (long long)rank * C;
+                if (slot < total) {
+                    values[slot] = (R)w[b + e];
+                    column[slot] = (int)(ke >> 32);
+                }
+            }
+        }
+    }
+}
+
+}  // namespace sbuild
 }  // namespace lgd
 
 using namespace lgd;
@@ -436,6 +610,167 @@ int lgd_sell_create(int n, int C, int64_t total, const int32_t *chunk_offset, co
             throw;
         }
         *out = reinterpret_cast<lgd_sell *>(s);
+    });
+}
+
+int lgd_sell_create_from_csr(int n, const int64_t *row_ptr, const int32_t *col, const double *w, int C, int sigma,
+                             int device_input, int precision, int flags, lgd_sell **out)
+{
+    return guard([&] {
+        using namespace sbuild;
+        LGD_REQUIRE(out != nullptr, LGD_ERR_INVALID, "null output");
+        *out = nullptr;
+        LGD_REQUIRE(n > 0, LGD_ERR_INVALID, "node count must be positive");
+        LGD_REQUIRE(C >= 1 && sigma >= 1, LGD_ERR_INVALID, "C and sigma must be at least 1");
+        LGD_REQUIRE(sigma <= LGD_SELL_GPU_MAX_SIGMA, LGD_ERR_UNSUPPORTED,
+                    "the device builder takes sigma <= 4096 (use lgd_sell_plan / lgd_sell_fill)");
+        LGD_REQUIRE(precision == 8 || precision == 4, LGD_ERR_INVALID, "precision must be 8 (FP64) or 4 (FP32)");
+        LGD_REQUIRE(row_ptr != nullptr, LGD_ERR_INVALID, "null row_ptr");
+        Sell *s = new Sell();
+        std::memset(s, 0, sizeof(Sell));
+        s->n = n;
+        s->C = C;
+        s->n_chunks = (n - 1) / C + 1;
+        s->rows_padded = s->n_chunks * C;
+        s->precision = precision;
+        s->flags = flags;
+        int64_t *d_rp = nullptr;
+        int32_t *d_col = nullptr;
+        double *d_w = nullptr;
+        int *d_len = nullptr, *d_inv = nullptr, *d_err = nullptr;
+        long long *d_total = nullptr;
+        auto release = [&] {
+            if (!device_input) {
+                cudaFree(d_rp);
+                cudaFree(d_col);
+                cudaFree(d_w);
+            }
+            cudaFree(d_len);
+            cudaFree(d_inv);
+            cudaFree(d_err);
+            cudaFree(d_total);
+        };
+        try {
+            LGD_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+            cudaStream_t st = s->stream;
+            long long nnz = 0;
+            if (device_input) {
+                d_rp = const_cast<int64_t *>(row_ptr);
+                d_col = const_cast<int32_t *>(col);
+                d_w = const_cast<double *>(w);
+                int64_t last = 0;
+                LGD_CHECK_CUDA(cudaMemcpyAsync(&last, row_ptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+                LGD_CHECK_CUDA(cudaStreamSynchronize(st));
+                nnz = last;
+            } else {
+                nnz = row_ptr[n];
+                LGD_CHECK_CUDA(cudaMalloc(&d_rp, sizeof(int64_t) * ((size_t)n + 1)));
+                LGD_CHECK_CUDA(cudaMemcpyAsync(d_rp, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+                if (nnz > 0) {
+                    LGD_REQUIRE(col && w, LGD_ERR_INVALID, "null matrix arrays");
+                    LGD_CHECK_CUDA(cudaMalloc(&d_col, sizeof(int32_t) * (size_t)nnz));
+                    LGD_CHECK_CUDA(cudaMalloc(&d_w, sizeof(double) * (size_t)nnz));
+                    LGD_CHECK_CUDA(cudaMemcpyAsync(d_col, col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+                    LGD_CHECK_CUDA(cudaMemcpyAsync(d_w, w, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+                }
+            }
+            LGD_REQUIRE(nnz >= 0, LGD_ERR_INVALID, "row_ptr must be non-decreasing");
+            LGD_REQUIRE(nnz == 0 || (d_col && d_w), LGD_ERR_INVALID, "null matrix arrays");
+            LGD_CHECK_CUDA(cudaMalloc(&d_len, sizeof(int) * (size_t)n));
+            LGD_CHECK_CUDA(cudaMalloc(&d_inv, sizeof(int) * (size_t)n));
+            LGD_CHECK_CUDA(cudaMalloc(&d_err, sizeof(int)));
+            LGD_CHECK_CUDA(cudaMalloc(&d_total, sizeof(long long)));
+            LGD_CHECK_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_perm, sizeof(int) * (size_t)n));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_row_length, sizeof(int) * (size_t)s->rows_padded));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_chunk_offset, sizeof(int) * ((size_t)s->n_chunks + 1)));
+            const int blocks = (int)std::min<long long>(152LL * 16, ((long long)s->rows_padded + 255) / 256);
+            lengths_kernel<<<blocks, 256, 0, st>>>(d_rp, n, d_len, d_err);
+            int P = 1;
+            while (P < std::min(sigma, n)) P <<= 1;
+            const int windows = (n + sigma - 1) / sigma;
+            window_sort_kernel<<<windows, SORT_THREADS, sizeof(uint32_t) * P, st>>>(d_len, n, sigma, P, s->d_perm);
+            row_length_kernel<<<blocks, 256, 0, st>>>(d_len, s->d_perm, n, s->rows_padded, s->d_row_length, d_inv);
+            chunk_scan_kernel<<<1, 1024, 0, st>>>(s->d_row_length, C, s->n_chunks, s->d_chunk_offset, d_total, d_err);
+            check_launch("sell build (plan)");
+            int err = 0;
+            long long total = 0;
+            LGD_CHECK_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+            LGD_CHECK_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(st));
+            LGD_REQUIRE(!(err & E_ROWPTR), LGD_ERR_INVALID, "row_ptr must start at 0 and be non-decreasing");
+            LGD_REQUIRE(!(err & E_LONGROW), LGD_ERR_UNSUPPORTED,
+                        "a row has more than 1024 entries (use lgd_sell_plan / lgd_sell_fill)");
+            LGD_REQUIRE(!(err & E_TOTAL), LGD_ERR_RANGE, "more than 2^31-1 SELL value slots");
+            s->total = total;
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_values, (size_t)precision * std::max<long long>(total, 1)));
+            LGD_CHECK_CUDA(cudaMalloc(&s->d_column, sizeof(int) * std::max<long long>(total, 1)));
+            LGD_CHECK_CUDA(cudaMemsetAsync(s->d_values, 0, (size_t)precision * std::max<long long>(total, 1), st));
+            LGD_CHECK_CUDA(cudaMemsetAsync(s->d_column, 0, sizeof(int) * std::max<long long>(total, 1), st));
+            if (nnz > 0) {
+                const int fblocks = (int)std::min<long long>(152LL * 64, ((long long)n + 7) / 8);
+                if (precision == 8) {
+                    fill_kernel<double><<<fblocks, 256, 0, st>>>(d_rp, d_col, d_w, s->d_perm, d_inv, s->d_chunk_offset,
+                                                                  n, C, total, (double *)s->d_values, s->d_column, d_err);
+                } else {
+                    fill_kernel<float><<<fblocks, 256, 0, st>>>(d_rp, d_col, d_w, s->d_perm, d_inv, s->d_chunk_offset,
+                                                                 n, C, total, (float *)s->d_values, s->d_column, d_err);
+                }
+                check_launch("sell build (fill)");
+            }
+            for (int bb = 0; bb < 2; ++bb) {
+                LGD_CHECK_CUDA(cudaMalloc(&s->d_x[bb], (size_t)precision * s->rows_padded));
+                LGD_CHECK_CUDA(cudaMemsetAsync(s->d_x[bb], 0, (size_t)precision * s->rows_padded, st));
+            }
+            LGD_CHECK_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(st));
+            LGD_REQUIRE(!(err & E_COLUMN), LGD_ERR_RANGE, "column id outside the node set");
+            release();
+        } catch (...) {
+            release();
+            sell_free(*s);
+            delete s;
+            throw;
+        }
+        *out = reinterpret_cast<lgd_sell *>(s);
+    });
+}
+
+int lgd_sell_get_layout(lgd_sell *h, int32_t *chunk_offset, int32_t *row_length, double *values, int32_t *column,
+                        int32_t *perm, int64_t *total)
+{
+    return guard([&] {
+        Sell& s = sell_of(h);
+        cudaStream_t st = s.stream;
+        if (total) *total = s.total;
+        if (chunk_offset) {
+            LGD_CHECK_CUDA(cudaMemcpyAsync(chunk_offset, s.d_chunk_offset, sizeof(int) * ((size_t)s.n_chunks + 1),
+                                           cudaMemcpyDeviceToHost, st));
+        }
+        if (row_length) {
+            LGD_CHECK_CUDA(cudaMemcpyAsync(row_length, s.d_row_length, sizeof(int) * (size_t)s.rows_padded,
+                                           cudaMemcpyDeviceToHost, st));
+        }
+        if (column && s.total > 0) {
+            LGD_CHECK_CUDA(cudaMemcpyAsync(column, s.d_column, sizeof(int) * (size_t)s.total, cudaMemcpyDeviceToHost, st));
+        }
+        if (perm) {
+            LGD_REQUIRE(s.d_perm != nullptr, LGD_ERR_INVALID, "the handle has no permutation");
+            LGD_CHECK_CUDA(cudaMemcpyAsync(perm, s.d_perm, sizeof(int) * (size_t)s.n, cudaMemcpyDeviceToHost, st));
+        }
+        if (values && s.total > 0) {
+            if (s.precision == 8) {
+                LGD_CHECK_CUDA(cudaMemcpyAsync(values, s.d_values, sizeof(double) * (size_t)s.total,
+                                               cudaMemcpyDeviceToHost, st));
+            } else {
+                std::vector<float> vf((size_t)s.total);
+                LGD_CHECK_CUDA(cudaMemcpyAsync(vf.data(), s.d_values, sizeof(float) * (size_t)s.total,
+                                               cudaMemcpyDeviceToHost, st));
+                LGD_CHECK_CUDA(cudaStreamSynchronize(st));
+                for (size_t i = 0; i < vf.size(); ++i) values[i] = vf[i];
+            }
+        }
+        LGD_CHECK_CUDA(cudaStreamSynchronize(st));
     });
 }
 

@@ -106,6 +106,8 @@ def lib():
             "lgd_sell_stream": [P, P],
             "lgd_sell_launch_count": [P, P],
             "lgd_sell_set_variant": [P, I],
+            "lgd_sell_create_from_csr": [I, P, P, P, I, I, I, I, I, P],
+            "lgd_sell_get_layout": [P, P, P, P, P, P, P],
             "lgd_lbm_create": [I, P, P, ctypes.c_double, I, P],
             "lgd_lbm_destroy": [P],
             "lgd_lbm_step": [P, I],
@@ -288,11 +290,57 @@ def sell_build(n: int, row_ptr, col, w, C: int, sigma: int, remap_columns: bool 
                 values=values[:t], column=column[:t], C=C, sigma=sigma, n=n)
 
 
+SELL_GPU_MAX_SIGMA = 4096     # LGD_SELL_GPU_MAX_SIGMA
+SELL_GPU_MAX_ROW = 1024       # LGD_SELL_GPU_MAX_ROW
+
+
 class SellGrid:
     """Device SELL-C-sigma grid running the diffusion cell."""
 
+    @classmethod
+    def from_csr(cls, n: int, row_ptr, col, w, C: int, sigma: int, precision: int = 8, exact: bool = False,
+                 device: bool = False):
+        """Builds the matrix on the GPU (lgd_sell_create_from_csr).  With
+        device=True the CSR arrays are torch CUDA tensors (int64, int32,
+        float64), else numpy arrays."""
+        self = cls.__new__(cls)
+        self.n = n
+        if device:
+            self._keep = [row_ptr, col, w]
+            ptrs = [ctypes.c_void_p(t.data_ptr()) for t in self._keep]
+        else:
+            self._keep = [np.ascontiguousarray(row_ptr, dtype=np.int64), np.ascontiguousarray(col, dtype=np.int32),
+                          np.ascontiguousarray(w, dtype=np.float64)]
+            ptrs = [_ptr(a) if a.size else ctypes.c_void_p() for a in self._keep]
+        self._h = ctypes.c_void_p()
+        self._C = C
+        check(lib().lgd_sell_create_from_csr(n, ptrs[0], ptrs[1], ptrs[2], C, sigma, int(device), precision,
+                                             SELL_EXACT if exact else 0, ctypes.byref(self._h)))
+        return self
+
+    def layout(self) -> dict:
+        """The device matrix as host arrays (chunk_offset, row_length,
+        values as FP64, column, perm)."""
+        total = ctypes.c_int64()
+        check(lib().lgd_sell_get_layout(self._h, None, None, None, None, None, ctypes.byref(total)))
+        t = total.value
+        C = self.C_of()
+        n_chunks = (self.n - 1) // C + 1
+        co = np.zeros(n_chunks + 1, dtype=np.int32)
+        rl = np.zeros(n_chunks * C, dtype=np.int32)
+        vals = np.zeros(max(t, 1), dtype=np.float64)
+        cols = np.zeros(max(t, 1), dtype=np.int32)
+        perm = np.zeros(self.n, dtype=np.int32)
+        check(lib().lgd_sell_get_layout(self._h, _ptr(co), _ptr(rl), _ptr(vals), _ptr(cols), _ptr(perm),
+                                        ctypes.byref(total)))
+        return dict(chunk_offset=co, row_length=rl, values=vals[:t], column=cols[:t], perm=perm)
+
+    def C_of(self) -> int:
+        return self._C
+
     def __init__(self, sell: dict, precision: int = 8, exact: bool = False):
         self.n = sell["n"]
+        self._C = sell["C"]
         self._keep = [np.ascontiguousarray(sell[k]) for k in ("chunk_offset", "row_length", "values", "column", "perm")]
         co, rl, vals, cols, perm = self._keep
         if vals.size == 0:
