@@ -12,9 +12,10 @@
 // honoured.  The simulator owns the Initializer, Writers and Steerers.
 //
 // Differences from CUDASimulator, all on the host <-> device path:
-//   - the grid is copied back to the host only when a Writer, a Steerer or
-//     getGrid() needs it (the reference copies the whole grid every time a
-//     writer asks, :490-497);
+//   - Writers get a read-only view that copies planes of the grid to the
+//     host when they touch them; Steerers and getGrid() get the whole grid,
+//     copied only when the device has moved on (the reference copies the
+//     whole grid every time a writer asks, :490-497);
 //   - after Steerers ran, the host grid is uploaded again, so steering
 //     changes reach the device (the reference leaves this as a fixme,
 //     :450-454);
@@ -84,6 +85,144 @@ inline void gb300Check(int rc)
     }
 }
 
+// Read-only view of the device grid handed to Writers.  A Writer that
+// reads part of the grid moves only that part: cells reach the host grid
+// plane by plane (3D: one z plane, 2D: a band of 64 rows, 1D: the line) on
+// first touch, through the library's streak copy (lgd_gpu_save_region),
+// and every plane is invalidated after a device step.  The reference's
+// CUDASimulator copies the whole grid for every writer call
+// (parallelization/cudasimulator.h:490-497).
+template<typename CELL, typename HostGrid>
+class GB300WriterView : public GridBase<CELL, HostGrid::DIM> {
+public:
+    static const int DIM = HostGrid::DIM;
+    static const int BAND = 64;             // rows per 2D band
+    typedef GB300CellTraits<CELL> Traits;
+
+    GB300WriterView(lgd_handle *const *handle, HostGrid *grid, const CoordBox<DIM>& box) :
+        handle(handle), grid(grid), box(box), valid(planes(), 1), fetched(0)
+    {}
+
+    void invalidate() { std::fill(valid.begin(), valid.end(), 0); }
+    void markAllValid() { std::fill(valid.begin(), valid.end(), 1); }
+    bool allValid() const { return std::find(valid.begin(), valid.end(), 0) == valid.end(); }
+    // bytes copied from the device by this view so far
+    std::size_t bytesFetched() const { return fetched; }
+
+    virtual CELL get(const Coord<DIM>& c) const
+    {
+        fetchFor(c);
+        return grid->get(c);
+    }
+    virtual void set(const Coord<DIM>&, const CELL&) { readOnly(); }
+    virtual void setEdge(const CELL&) { readOnly(); }
+    virtual const CELL& getEdge() const { return grid->getEdge(); }
+    virtual CoordBox<DIM> boundingBox() const { return grid->boundingBox(); }
+
+#ifdef LGD_GB300_WITH_REFERENCE
+    virtual void resize(const CoordBox<DIM>&) { readOnly(); }
+    virtual void set(const Streak<DIM>&, const CELL *) { readOnly(); }
+    virtual void get(const Streak<DIM>& s, CELL *cells) const
+    {
+        fetchFor(s.origin);
+        grid->get(s, cells);
+    }
+    virtual void saveRegion(std::vector<CELL> *buffer, const Region<DIM>& region,
+                            const Coord<DIM>& offset = Coord<DIM>()) const
+    {
+        for (typename Region<DIM>::StreakIterator i = region.beginStreak(); i != region.endStreak(); ++i) {
+            fetchFor(i->origin + offset);
+        }
+        grid->saveRegion(buffer, region, offset);
+    }
+
+protected:
+    virtual void saveMemberImplementation(char *target, MemoryLocation::Location targetLocation,
+                                          const Selector<CELL>& selector,
+                                          const typename Region<DIM>::StreakIterator& begin,
+                                          const typename Region<DIM>::StreakIterator& end) const
+    {
+        Region<DIM> region;
+        for (typename Region<DIM>::StreakIterator i = begin; i != end; ++i) {
+            fetchFor(i->origin);
+            region << *i;
+        }
+        grid->saveMember(target, targetLocation, selector, region);
+    }
+    virtual void loadMemberImplementation(const char *, MemoryLocation::Location, const Selector<CELL>&,
+                                          const typename Region<DIM>::StreakIterator&,
+                                          const typename Region<DIM>::StreakIterator&)
+    {
+        readOnly();
+    }
+#endif
+
+private:
+    lgd_handle *const *handle;      // the simulator's handle (it may be re-created)
+    HostGrid *grid;
+    CoordBox<DIM> box;
+    mutable std::vector<char> valid;
+    mutable std::size_t fetched;
+
+    static void readOnly() { throw std::logic_error("the writers' view of a GB300 grid is read-only"); }
+
+    int planes() const
+    {
+        if (DIM == 3) return box.dimensions[2];
+        if (DIM == 2) return (box.dimensions[1] + BAND - 1) / BAND;
+        return 1;
+    }
+
+    void fetchFor(const Coord<DIM>& c) const
+    {
+        for (int d = 0; d < DIM; ++d) {
+            if (c[d] < box.origin[d] || c[d] >= box.origin[d] + box.dimensions[d]) return;   // the edge cell
+        }
+        const int p = (DIM == 3) ? c[2] - box.origin[2] : (DIM == 2) ? (c[1] - box.origin[1]) / BAND : 0;
+        if (!valid[p]) fetchPlane(p);
+    }
+
+    // every row of plane p, all members, in one streak copy per member
+    void fetchPlane(int p) const
+    {
+        const int nx = box.dimensions[0];
+        const int ny = DIM > 1 ? box.dimensions[1] : 1;
+        const int y0 = (DIM == 2) ? p * BAND : 0;
+        const int y1 = (DIM == 2) ? std::min(ny, y0 + BAND) : ny;
+        const int z = (DIM == 3) ? p : 0;
+        std::vector<int> streaks;
+        for (int y = y0; y < y1; ++y) {
+            streaks.push_back(0);
+            streaks.push_back(y);
+            streaks.push_back(z);
+            streaks.push_back(nx);
+        }
+        const int rows = y1 - y0;
+        const std::size_t cells = (std::size_t)rows * nx;
+        std::vector<std::vector<char> > bufs(Traits::MEMBERS);
+        for (int m = 0; m < Traits::MEMBERS; ++m) {
+            bufs[m].resize(cells * Traits::memberSize(m));
+            gb300Check(lgd_gpu_save_region(*handle, m, streaks.data(), rows, bufs[m].data(), bufs[m].size()));
+            fetched += bufs[m].size();
+        }
+        std::size_t i = 0;
+        for (int y = y0; y < y1; ++y) {
+            for (int x = 0; x < nx; ++x, ++i) {
+                Coord<DIM> c = box.origin;
+                c[0] += x;
+                if (DIM > 1) c[1] += y;
+                if (DIM > 2) c[2] += z;
+                CELL cell = grid->get(c);
+                for (int m = 0; m < Traits::MEMBERS; ++m) {
+                    Traits::unpack(&cell, m, &bufs[m][i * Traits::memberSize(m)]);
+                }
+                grid->set(c, cell);
+            }
+        }
+        valid[p] = 1;
+    }
+};
+
 template<typename CELL>
 class GB300Simulator : public MonolithicSimulator<CELL> {
 public:
@@ -99,7 +238,7 @@ public:
         MonolithicSimulator<CELL>(initializer),
         handle(0),
         hostGrid(0),
-        hostStale(false)
+        view(0)
     {
         if (blockSize.x() <= 0 || blockSize.y() <= 0 || blockSize.z() <= 0) {
             throw std::invalid_argument("blockSize must be positive");
@@ -109,6 +248,7 @@ public:
         simArea << box;
         hostGrid = new HostGrid(box);
         initializer->grid(hostGrid);
+        view = new WriterView(&handle, hostGrid, box);
         createDevice();
         upload();
     }
@@ -116,6 +256,7 @@ public:
     virtual ~GB300Simulator()
     {
         if (handle) lgd_gpu_destroy(handle);
+        delete view;
         delete hostGrid;
     }
 
@@ -131,7 +272,7 @@ public:
         for (unsigned i = 0; i < NANO_STEPS; ++i) {
             gb300Check(lgd_gpu_step(handle, i, 1));
         }
-        hostStale = true;
+        view->invalidate();
         ++this->stepNum;
         WriterEvent event = WRITER_STEP_FINISHED;
         if (this->stepNum == this->initializer->maxSteps()) {
@@ -143,7 +284,7 @@ public:
     virtual void run()
     {
         this->initializer->grid(hostGrid);
-        hostStale = false;
+        view->markAllValid();
         this->stepNum = this->initializer->startStep();
         if (edgeChanged()) {
             gb300Check(lgd_gpu_destroy(handle));
@@ -174,12 +315,17 @@ public:
     // The library handle, for callers that want the device grid directly.
     lgd_handle *deviceHandle() { return handle; }
 
+    // Bytes the Writers' view has copied from the device (Writers that read
+    // part of the grid move only that part).
+    std::size_t writerBytesFetched() const { return view->bytesFetched(); }
+
 private:
+    typedef GB300WriterView<CELL, HostGrid> WriterView;
     lgd_handle *handle;
     HostGrid *hostGrid;
+    WriterView *view;       // the host grid's validity, plane by plane
     CoordBox<DIM> box;
     Region<DIM> simArea;
-    bool hostStale;
     double edge[4];
 
     void createDevice()
@@ -223,12 +369,13 @@ private:
             }
             gb300Check(lgd_gpu_upload(handle, m, 0, buf.data(), buf.size()));
         }
-        hostStale = false;
+        view->markAllValid();
     }
 
+    // the whole grid to the host (unless every plane is there already)
     void download()
     {
-        if (!hostStale) return;
+        if (view->allValid()) return;
         const std::size_t n = box.size();
         std::vector<std::vector<char> > bufs(Traits::MEMBERS);
         for (int m = 0; m < Traits::MEMBERS; ++m) {
@@ -243,7 +390,7 @@ private:
             }
             hostGrid->set(*c, cell);
         }
-        hostStale = false;
+        view->markAllValid();
     }
 
     // Steps before the next one that calls a plugin: no Steerer runs before
@@ -269,7 +416,7 @@ private:
         if (next <= s) return;
         gb300Check(lgd_gpu_step(handle, 0, (int)std::min<unsigned>(next - s, 1u << 30)));
         this->stepNum = next;
-        hostStale = true;
+        view->invalidate();
     }
 
     void handleInput(SteererEvent event, SteererFeedback *feedback)
@@ -290,7 +437,7 @@ private:
     {
         for (std::size_t i = 0; i < this->writers.size(); ++i) {
             if ((event != WRITER_STEP_FINISHED) || ((this->getStep() % this->writers[i]->getPeriod()) == 0)) {
-                this->writers[i]->stepFinished(*getGrid(), this->getStep(), event);
+                this->writers[i]->stepFinished(*view, this->getStep(), event);   // planes on demand
             }
         }
     }

@@ -231,6 +231,50 @@ static void testManualStepsMatchCpu()
     EXPECT(sim.getStep() == 7);
 }
 
+// A writer that reads one cell per call: the view it gets copies one z plane
+// per call, not the grid.
+class ProbeWriter : public Writer<JacobiCell> {
+public:
+    ProbeWriter(unsigned period, Coord<3> probe, std::vector<double> *seen) :
+        Writer<JacobiCell>("probe", period), probe(probe), seen(seen)
+    {}
+    Writer<JacobiCell> *clone() const { return new ProbeWriter(period, probe, seen); }
+    void stepFinished(const GridType& grid, unsigned, WriterEvent) { seen->push_back(grid.get(probe).temp); }
+
+private:
+    Coord<3> probe;
+    std::vector<double> *seen;
+};
+
+static void testWriterReadsOnlyWhatItTouches()
+{
+    const Coord<3> dim(19, 11, 17);
+    const Coord<3> probe(5, 7, 9);
+    std::vector<double> seen;
+    GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 9));
+    sim.addWriter(new ProbeWriter(3, probe, &seen));
+    sim.run();
+    // INITIALIZED@0, STEP_FINISHED@3, @6, ALL_DONE@9
+    EXPECT(seen.size() == 4);
+    const int at[4] = {0, 3, 6, 9};
+    for (std::size_t k = 0; k < seen.size() && k < 4; ++k) {
+        std::vector<double> ref = cpuJacobi(dim, at[k]);
+        EXPECT(seen[k] == ref[((std::size_t)probe.z() * dim.y() + probe.y()) * dim.x() + probe.x()]);
+    }
+    // the initial grid is on the host; afterwards one plane per call
+    const std::size_t plane = (std::size_t)dim.x() * dim.y() * sizeof(double);
+    EXPECT(sim.writerBytesFetched() == 3 * plane);
+    // getGrid() still gives the whole grid, current
+    std::vector<double> ref = cpuJacobi(dim, 9);
+    const GridBase<JacobiCell, 3> *g = sim.getGrid();
+    int mismatches = 0;
+    std::size_t i = 0;
+    for (int z = 0; z < dim.z(); ++z)
+        for (int y = 0; y < dim.y(); ++y)
+            for (int x = 0; x < dim.x(); ++x, ++i) mismatches += (g->get(Coord<3>(x, y, z)).temp != ref[i]);
+    EXPECT(mismatches == 0);
+}
+
 static void testBadBlockSizeThrows()
 {
     bool thrown = false;
@@ -304,6 +348,7 @@ int main()
     testSteeringReachesDevice();
     testManualStepsMatchCpu();
     testBadBlockSizeThrows();
+    testWriterReadsOnlyWhatItTouches();
     testGliderCrossesTorus();
     if (failures) {
         std::printf("%d failure(s)\n", failures);
