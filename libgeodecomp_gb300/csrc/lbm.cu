@@ -2,7 +2,12 @@
 //
 // All instances live in one pair of allocations (A, B), each instance as
 // structure of arrays: population i of cell (x, y, z) of an L^3 instance at
-// base + i * L^3 + (z * L + y) * L + x.  Every time step is one persistent
+// base + i * P + (z * L + y) * L + x, with the population pitch P = L^3
+// rounded up to 32 elements and every base a multiple of 32, so each
+// population array starts on a 128-byte (FP32) boundary.  Warps walk the
+// cells of a work item in 32-cell groups aligned to that boundary (lanes
+// outside the item idle), so a warp's own-cell loads and stores are whole
+// sectors.  Every time step is one persistent
 // kernel launch: the CTAs pull work items - TY rows of one z plane of one
 // instance, largest instances first - from an atomic counter until the list
 // is exhausted, so instances of 32^3 and 192^3 cells share the GPU without
@@ -30,6 +35,7 @@ namespace lgd {
 
 struct LbmInstance {
     long long base;     // element offset of the instance in A and B
+    long long pitch;    // elements between populations: L^3 rounded up to 32
     int L;
     unsigned magic;     // ceil(2^32 / L), for row = c / L
     float omega_f;
@@ -127,14 +133,17 @@ struct Mem {
     }
 };
 
-template<typename R, int I, typename IDX, int NC>
+// INTERIOR: the cell is at least one cell away from every wall, so every
+// source cell exists (no wall tests)
+template<typename R, int I, typename IDX, int NC, bool INTERIOR>
 __device__ __forceinline__ void pull_one(const R *__restrict__ src, IDX n3, IDX cell, int L, int x, int y,
                                          int z, R lid, R *f)
 {
     const int sx = x - Q<I>::ex;
     const int sy = y - Q<I>::ey;
     const int sz = z - Q<I>::ez;
-    if ((unsigned)sx < (unsigned)L && (unsigned)sy < (unsigned)L && (unsigned)sz < (unsigned)L) {
+    if (INTERIOR ||
+        ((unsigned)sx < (unsigned)L && (unsigned)sy < (unsigned)L && (unsigned)sz < (unsigned)L)) {
         f[I] = Mem<NC>::ld(src + (I * n3 + cell - (Q<I>::ex + (IDX)Q<I>::ey * L + (IDX)Q<I>::ez * L * L)));
     } else {
         const R w = (I == 0) ? (R)(1.0 / 3.0) : ((I < 7) ? (R)(1.0 / 18.0) : (R)(1.0 / 36.0));
@@ -148,17 +157,17 @@ __device__ __forceinline__ void pull_one(const R *__restrict__ src, IDX n3, IDX 
     }
 }
 
-template<typename R, int I, typename IDX, int NC>
+template<typename R, int I, typename IDX, int NC, bool INTERIOR>
 struct PullAll {
     static __device__ __forceinline__ void run(const R *src, IDX n3, IDX cell, int L, int x, int y, int z, R lid, R *f)
     {
-        pull_one<R, I, IDX, NC>(src, n3, cell, L, x, y, z, lid, f);
-        PullAll<R, I + 1, IDX, NC>::run(src, n3, cell, L, x, y, z, lid, f);
+        pull_one<R, I, IDX, NC, INTERIOR>(src, n3, cell, L, x, y, z, lid, f);
+        PullAll<R, I + 1, IDX, NC, INTERIOR>::run(src, n3, cell, L, x, y, z, lid, f);
     }
 };
 
-template<typename R, typename IDX, int NC>
-struct PullAll<R, 19, IDX, NC> {
+template<typename R, typename IDX, int NC, bool INTERIOR>
+struct PullAll<R, 19, IDX, NC, INTERIOR> {
     static __device__ __forceinline__ void run(const R *, IDX, IDX, int, int, int, int, R, R *) {}
 };
 
@@ -196,27 +205,47 @@ __device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict
 }
 
 // Cells of rows [y0, y1) of plane z (contiguous in memory), the threads
-// first, first + stride, ... of the group taking cells in that order.  IDX
-// is the index type inside one instance: 32-bit when 19 L^3 < 2^31.
+// first, first + stride, ... of the group taking cells in that order,
+// starting at the 32-cell boundary at or before the first cell (stride a
+// multiple of 32).  IDX is the index type inside one instance: 32-bit when
+// 19 P < 2^31.
 template<typename R, typename IDX, int NC>
 __device__ __forceinline__ void lbm_item(const LbmInstance& in, const R *__restrict__ A, R *__restrict__ B, int z, int y0,
                                          int y1, unsigned first, unsigned stride)
 {
     const int L = in.L;
-    const IDX n3 = (IDX)L * L * L;
+    // the population pitch (LbmInstance::pitch), recomputed from L: a
+    // loaded pitch makes the compiler keep the 38 addresses live (128
+    // registers instead of 56)
+    const IDX n3 = ((IDX)L * L * L + 31) & ~(IDX)31;
     const R *src = A + in.base;
     R *dst = B + in.base;
     const R omega = (sizeof(R) == 8) ? (R)in.omega : (R)in.omega_f;
     const R lid = (sizeof(R) == 8) ? (R)in.lid : (R)in.lid_f;
-    const unsigned cells = (unsigned)(y1 - y0) * (unsigned)L;
-    for (unsigned c = first; c < cells; c += stride) {
+    // plane-relative cell indices [cb, ce); the walk starts at the 32-cell
+    // boundary at or before cb (a negative start stays in the plane before)
+    const int cb = y0 * L;
+    const int ce = y1 * L;
+    const int lead = (int)((((IDX)z * L * L) + cb) & 31);
+    int k0 = cb - lead + (int)first;
+    if (k0 < cb) k0 += (int)stride;                     // lanes before the item start one round later
+    for (int k = k0; k < ce; k += (int)stride) {
+        const unsigned c = (unsigned)k;                 // index inside the plane
         unsigned r = __umulhi(c, in.magic);
         if (r * (unsigned)L > c) --r;
-        const int y = y0 + (int)r;
+        const int y = (int)r;
         const int x = (int)(c - r * (unsigned)L);
+        // the cell index rebuilt from (x, y, z), not the loop counter: the
+        // 38 addresses are then recomputed per cell instead of being kept
+        // as induction variables (56 registers instead of 128)
         const IDX cell = ((IDX)z * L + y) * L + x;
         R f[19];
-        PullAll<R, 0, IDX, NC>::run(src, n3, cell, L, x, y, z, lid, f);
+        if ((unsigned)(x - 1) < (unsigned)(L - 2) && (unsigned)(y - 1) < (unsigned)(L - 2) &&
+            (unsigned)(z - 1) < (unsigned)(L - 2)) {
+            PullAll<R, 0, IDX, NC, true>::run(src, n3, cell, L, x, y, z, lid, f);
+        } else {
+            PullAll<R, 0, IDX, NC, false>::run(src, n3, cell, L, x, y, z, lid, f);
+        }
         collide_store<R, IDX, NC>(f, omega, dst, n3, cell);
     }
 }
@@ -261,10 +290,11 @@ __global__ void lbm_rest_kernel(const LbmInstance *__restrict__ inst, int count,
     if (j >= count) return;
     const LbmInstance in = inst[j];
     const long long n3 = (long long)in.L * in.L * in.L;
+    const long long P = in.pitch;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n3; c += (long long)gridDim.x * blockDim.x) {
         A[in.base + c] = (R)(1.0 / 3.0);
-        for (int i = 1; i < 7; ++i) A[in.base + i * n3 + c] = (R)(1.0 / 18.0);
-        for (int i = 7; i < 19; ++i) A[in.base + i * n3 + c] = (R)(1.0 / 36.0);
+        for (int i = 1; i < 7; ++i) A[in.base + i * P + c] = (R)(1.0 / 18.0);
+        for (int i = 7; i < 19; ++i) A[in.base + i * P + c] = (R)(1.0 / 36.0);
     }
 }
 
@@ -460,9 +490,10 @@ int lgd_lbm_create(int count, const int32_t *edges, const double *omegas, double
             in.omega_f = (float)omegas[j];
             in.lid_f = (float)lid;
             const long long n3 = (long long)edges[j] * edges[j] * edges[j];
-            off += 19 * n3;
+            in.pitch = (n3 + 31) / 32 * 32;
+            off += 19 * in.pitch;
             e->total_cells += n3;
-            if (19 * n3 >= (1ll << 31)) e->idx32 = false;
+            if (19 * in.pitch >= (1ll << 31)) e->idx32 = false;
             LGD_REQUIRE(n3 * 19 < (1ll << 31) * 16, LGD_ERR_RANGE, "instance too large");
         }
         e->total_elems = off;
@@ -632,13 +663,15 @@ int lgd_lbm_download(lgd_lbm *h, int instance, double *f, size_t bytes)
         const LbmInstance& in = e.inst[instance];
         const size_t n = 19ull * in.L * in.L * in.L;
         LGD_REQUIRE(f != nullptr && bytes == n * sizeof(double), LGD_ERR_INVALID, "buffer must hold 19 * L^3 doubles");
+        const size_t n3 = n / 19;
         if (e.precision == 8) {
-            LGD_CHECK_CUDA(cudaMemcpyAsync(f, (const double *)e.buf[e.cur] + in.base, bytes, cudaMemcpyDeviceToHost, e.stream));
+            LGD_CHECK_CUDA(cudaMemcpy2DAsync(f, n3 * 8, (const double *)e.buf[e.cur] + in.base, (size_t)in.pitch * 8,
+                                             n3 * 8, 19, cudaMemcpyDeviceToHost, e.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
         } else {
             std::vector<float> tmp(n);
-            LGD_CHECK_CUDA(cudaMemcpyAsync(tmp.data(), (const float *)e.buf[e.cur] + in.base, n * 4, cudaMemcpyDeviceToHost,
-                                           e.stream));
+            LGD_CHECK_CUDA(cudaMemcpy2DAsync(tmp.data(), n3 * 4, (const float *)e.buf[e.cur] + in.base,
+                                             (size_t)in.pitch * 4, n3 * 4, 19, cudaMemcpyDeviceToHost, e.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
             for (size_t i = 0; i < n; ++i) f[i] = tmp[i];
         }
@@ -653,13 +686,15 @@ int lgd_lbm_upload(lgd_lbm *h, int instance, const double *f, size_t bytes)
         const LbmInstance& in = e.inst[instance];
         const size_t n = 19ull * in.L * in.L * in.L;
         LGD_REQUIRE(f != nullptr && bytes == n * sizeof(double), LGD_ERR_INVALID, "buffer must hold 19 * L^3 doubles");
+        const size_t n3 = n / 19;
         if (e.precision == 8) {
-            LGD_CHECK_CUDA(cudaMemcpyAsync((double *)e.buf[e.cur] + in.base, f, bytes, cudaMemcpyHostToDevice, e.stream));
+            LGD_CHECK_CUDA(cudaMemcpy2DAsync((double *)e.buf[e.cur] + in.base, (size_t)in.pitch * 8, f, n3 * 8, n3 * 8, 19,
+                                             cudaMemcpyHostToDevice, e.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
         } else {
             std::vector<float> tmp(f, f + n);
-            LGD_CHECK_CUDA(cudaMemcpyAsync((float *)e.buf[e.cur] + in.base, tmp.data(), n * 4, cudaMemcpyHostToDevice,
-                                           e.stream));
+            LGD_CHECK_CUDA(cudaMemcpy2DAsync((float *)e.buf[e.cur] + in.base, (size_t)in.pitch * 4, tmp.data(), n3 * 4,
+                                             n3 * 4, 19, cudaMemcpyHostToDevice, e.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
         }
     });
