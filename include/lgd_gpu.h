@@ -198,6 +198,15 @@ int lgd_gpu_stream(lgd_handle *h, void **stream);
 #define LGD_SUM_STATIC_MAX_N (1LL << 30)
 int lgd_sum_f64_static(const double *d_values, long long n, double *d_result, void *stream);
 
+/* Writes one member of the current grid as a BOV snapshot, straight from
+ * the device: header prefix.<step, 5 digits>.bov and raw little-endian
+ * data prefix.<step>.data, x fastest, in the format of the reference's
+ * SerialBOVWriter (io/serialbovwriter.h, io/bovoutput.h:17-58): DATA_FORMAT
+ * DOUBLE, FLOAT or BYTE by the member's type, 2D grids as nz = 1, one
+ * brick, one component, VARIABLE the given name.  Fixed-point grids write
+ * their FP64 values.  Synchronises the handle's stream. */
+int lgd_gpu_write_bov(lgd_handle *h, int member, const char *prefix, unsigned step, const char *variable);
+
 /* Sum of one member over the whole grid in FP64 (deterministic order). */
 int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum);
 

@@ -2,6 +2,7 @@
 // copies, stepping, region updates.  See include/lgd_gpu.h for the
 // contract and the reference entry points each function replaces.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -417,6 +418,43 @@ int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t by
                                          cudaMemcpyDeviceToHost, g.stream));
         LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
         check_device_error(g);
+    });
+}
+
+int lgd_gpu_write_bov(lgd_handle *h, int member, const char *prefix, unsigned step, const char *variable)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, 0);
+        LGD_REQUIRE(prefix != nullptr && variable != nullptr, LGD_ERR_INVALID, "null file prefix or variable name");
+        const size_t n = cells_of(g);
+        const int elem = g.m[member].elem;
+        std::vector<unsigned char> data(n * elem);
+        const int rc = lgd_gpu_download(h, member, 0, data.data(), data.size());
+        LGD_REQUIRE(rc == LGD_OK, rc, "download for the BOV snapshot failed");
+        const char *format = (elem == 8) ? "DOUBLE" : (elem == 4) ? "FLOAT" : "BYTE";
+        char stepbuf[32];
+        std::snprintf(stepbuf, sizeof(stepbuf), "%05u", step);
+        const std::string stem = std::string(prefix) + "." + stepbuf;
+        const std::string header_name = stem + ".bov";
+        const std::string data_name = stem + ".data";
+        char dims[96];
+        std::snprintf(dims, sizeof(dims), "%d %d %d", g.desc.nx, g.desc.ny, g.desc.nz);
+        const std::string header = std::string("TIME: ") + std::to_string(step) + "\n" + "DATA_FILE: " + data_name + "\n" +
+                                   "DATA_SIZE: " + dims + "\n" + "DATA_FORMAT: " + format + "\n" + "VARIABLE: " +
+                                   variable + "\n" + "DATA_ENDIAN: LITTLE\n" + "BRICK_ORIGIN: 0 0 0\n" +
+                                   "BRICK_SIZE: " + dims + "\n" + "DIVIDE_BRICK: true\n" + "DATA_BRICKLETS: " + dims +
+                                   "\n" + "DATA_COMPONENTS: 1\n";
+        FILE *f = std::fopen(header_name.c_str(), "wb");
+        LGD_REQUIRE(f != nullptr, LGD_ERR_INVALID, "cannot open " + header_name);
+        const bool ok1 = std::fwrite(header.data(), 1, header.size(), f) == header.size();
+        const bool ok2 = std::fclose(f) == 0;
+        LGD_REQUIRE(ok1 && ok2, LGD_ERR_INVALID, "cannot write " + header_name);
+        f = std::fopen(data_name.c_str(), "wb");
+        LGD_REQUIRE(f != nullptr, LGD_ERR_INVALID, "cannot open " + data_name);
+        const bool ok3 = std::fwrite(data.data(), 1, data.size(), f) == data.size();
+        const bool ok4 = std::fclose(f) == 0;
+        LGD_REQUIRE(ok3 && ok4, LGD_ERR_INVALID, "cannot write " + data_name);
     });
 }
 

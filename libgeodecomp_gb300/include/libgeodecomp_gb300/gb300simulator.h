@@ -443,6 +443,35 @@ private:
     }
 };
 
+// Writer plugin that writes BOV snapshots of one member straight from the
+// device grid of a GB300Simulator (lgd_gpu_write_bov): the format of the
+// reference's SerialBOVWriter (io/serialbovwriter.h), without copying the
+// grid into host cells first.  The simulator owns the writer (addWriter),
+// so the pointer it keeps stays valid.
+template<typename CELL>
+class GB300BOVWriter : public Writer<CELL> {
+public:
+    typedef typename Writer<CELL>::GridType GridType;
+
+    GB300BOVWriter(GB300Simulator<CELL> *sim, int member, const std::string& variable, const std::string& prefix,
+                   unsigned period) :
+        Writer<CELL>(prefix, period), sim(sim), member(member), variable(variable)
+    {}
+
+    Writer<CELL> *clone() const { return new GB300BOVWriter(sim, member, variable, this->prefix, this->period); }
+
+    void stepFinished(const GridType&, unsigned step, WriterEvent event)
+    {
+        if ((event == WRITER_STEP_FINISHED) && (step % this->period != 0)) return;
+        gb300Check(lgd_gpu_write_bov(sim->deviceHandle(), member, this->prefix.c_str(), step, variable.c_str()));
+    }
+
+private:
+    GB300Simulator<CELL> *sim;
+    int member;
+    std::string variable;
+};
+
 }  // namespace LibGeoDecomp
 
 #endif

@@ -91,6 +91,7 @@ def lib():
             "lgd_gpu_launch_count": [P, P],
             "lgd_gpu_set_time_block": [P, I],
             "lgd_gpu_set_time_block_shape": [P, I],
+            "lgd_gpu_write_bov": [P, I, ctypes.c_char_p, ctypes.c_uint, ctypes.c_char_p],
             "lgd_gpu_set_variant": [P, I],
             "lgd_gpu_stream": [P, P],
             "lgd_sell_plan": [I, P, I, I, P, P, P, P, P],
@@ -248,6 +249,10 @@ class Grid:
 
     def set_time_block(self, depth: int):
         check(lib().lgd_gpu_set_time_block(self._h, depth))
+
+    def write_bov(self, prefix: str, step: int, member: int = 0, variable: str = "var"):
+        """BOV snapshot of one member straight from the device (prefix.<step>.bov / .data)."""
+        check(lib().lgd_gpu_write_bov(self._h, member, prefix.encode(), step, variable.encode()))
 
     def set_time_block_shape(self, shape: int):
         check(lib().lgd_gpu_set_time_block_shape(self._h, shape))

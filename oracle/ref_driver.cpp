@@ -25,6 +25,7 @@
  */
 #include <libgeodecomp/config.h>
 #include <libgeodecomp/geometry/stencils.h>
+#include <libgeodecomp/io/serialbovwriter.h>
 #include <libgeodecomp/io/simpleinitializer.h>
 #include <libgeodecomp/misc/apitraits.h>
 #include <libgeodecomp/parallelization/serialsimulator.h>
@@ -177,6 +178,22 @@ static int runJacobi(Coord<3> dim, unsigned steps, const char *in, const char *o
         }
     }
     writeArray(out, result);
+    return 0;
+}
+
+// The reference's SerialBOVWriter (io/serialbovwriter.h, io/bovoutput.h) on
+// the Jacobi cube cell: run() with a writer of period `steps` writes
+// prefix.00000.{bov,data} (WRITER_INITIALIZED) and prefix.<steps>.{bov,data}
+// (WRITER_STEP_FINISHED, then WRITER_ALL_DONE to the same files).
+template<typename CELL>
+static int runBov(Coord<3> dim, unsigned steps, const char *in, const char *prefix)
+{
+    std::size_t n = std::size_t(dim.x()) * dim.y() * dim.z();
+    std::vector<double> values = readArray<double>(in, n);
+    SerialSimulator<CELL> sim(new ArrayInitializer3D<CELL>(dim, steps, &values));
+    sim.addWriter(new SerialBOVWriter<CELL>(Selector<CELL>(&CELL::temp, "temp"), prefix, steps));
+    sim.run();
+    std::printf("{}\n");
     return 0;
 }
 
@@ -693,6 +710,10 @@ static int dispatch(int argc, char **argv)
         }
         return omp ? runJacobi<Jacobi7CubeCell, OpenMPSimulator<Jacobi7CubeCell> >(dim, steps, argv[7], argv[8], timeOnly(10))
                    : runJacobi<Jacobi7CubeCell, SerialSimulator<Jacobi7CubeCell> >(dim, steps, argv[7], argv[8], timeOnly(10));
+    }
+    if (cmd == "bov" && argc >= 8) {
+        Coord<3> dim(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]));
+        return runBov<Jacobi7CubeCell>(dim, std::atoi(argv[5]), argv[6], argv[7]);
     }
     if (cmd == "gol" && argc >= 8) {
         Coord<2> dim(std::atoi(argv[2]), std::atoi(argv[3]));

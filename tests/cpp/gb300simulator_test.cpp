@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 using namespace LibGeoDecomp;
@@ -275,6 +276,35 @@ static void testWriterReadsOnlyWhatItTouches()
     EXPECT(mismatches == 0);
 }
 
+// BOV snapshots straight from the device: at the start and every 4 steps,
+// the data file holds the grid of that step
+static void testBovWriterFromDevice()
+{
+    const Coord<3> dim(12, 9, 7);
+    const std::string prefix = "gb300_bov_test";
+    {
+        GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 8));
+        sim.addWriter(new GB300BOVWriter<JacobiCell>(&sim, 0, "temp", prefix, 4));
+        sim.run();
+    }
+    const std::size_t n = (std::size_t)dim.x() * dim.y() * dim.z();
+    const int at[3] = {0, 4, 8};
+    for (int k = 0; k < 3; ++k) {
+        char name[128];
+        std::snprintf(name, sizeof(name), "%s.%05d.data", prefix.c_str(), at[k]);
+        std::vector<double> got(n);
+        FILE *f = std::fopen(name, "rb");
+        EXPECT(f != nullptr);
+        if (!f) continue;
+        EXPECT(std::fread(got.data(), sizeof(double), n, f) == n);
+        std::fclose(f);
+        std::remove(name);
+        std::snprintf(name, sizeof(name), "%s.%05d.bov", prefix.c_str(), at[k]);
+        EXPECT(std::remove(name) == 0);
+        EXPECT(got == cpuJacobi(dim, at[k]));
+    }
+}
+
 static void testBadBlockSizeThrows()
 {
     bool thrown = false;
@@ -349,6 +379,7 @@ int main()
     testManualStepsMatchCpu();
     testBadBlockSizeThrows();
     testWriterReadsOnlyWhatItTouches();
+    testBovWriterFromDevice();
     testGliderCrossesTorus();
     if (failures) {
         std::printf("%d failure(s)\n", failures);

@@ -68,6 +68,25 @@ def jacobi(tmp, name, topo, nx, ny, nz, steps, full=True):
                         torus=np.array(topo == "torus"), seed=np.array(42), u0_sha256=np.array(sha(u0)), **extra)
 
 
+def bov(tmp, name, nx, ny, nz, steps):
+    """Header and data files of the reference's SerialBOVWriter for the
+    Jacobi cube cell at step 0 and at step `steps` (prefix "jac", relative
+    to the working directory, as DATA_FILE records it)."""
+    u0 = workloads.jacobi_initial(nx, ny, nz, seed=42)
+    fin = os.path.join(tmp, "in.f64")
+    u0.tofile(fin)
+    run(["bov", nx, ny, nz, steps, fin, "jac"], tmp)
+    files = {}
+    for step in (0, steps):
+        stem = os.path.join(tmp, "jac.%05d" % step)
+        with open(stem + ".bov", "rb") as f:
+            files["bov_%d" % step] = np.frombuffer(f.read(), dtype=np.uint8)
+        with open(stem + ".data", "rb") as f:
+            files["data_%d" % step] = np.frombuffer(f.read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), shape=np.array([nz, ny, nx]), steps=np.array(steps),
+                        seed=np.array(42), u0_sha256=np.array(sha(u0)), **files)
+
+
 def gol(tmp, name, nx, ny, steps, full=True):
     c0 = workloads.gol_initial(nx, ny, seed=42)
     fin = os.path.join(tmp, "in.u8")
@@ -207,6 +226,7 @@ def main():
         lbm(tmp, "lbm_L8", 8, 30, 1.7, 0.05)
         lbm(tmp, "lbm_L24", 24, 100, 1.2, 0.05, full=False)
         varcoef(tmp, "varcoef_16", 16, 20, 4.0)
+        bov(tmp, "bov_jacobi_24x20x16", 24, 20, 16, 6)
     print("fixtures written to", OUT)
 
 

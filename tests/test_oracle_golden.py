@@ -152,3 +152,17 @@ def test_oracle_thread_count_does_not_change_results():
     a = oracle.jacobi7(u0, 5, threads=1)
     b = oracle.jacobi7(u0, 5, threads=4)
     np.testing.assert_array_equal(a, b)
+
+
+def test_bov_fixture_matches_oracle_and_format():
+    """The reference's SerialBOVWriter files: data = the oracle's Jacobi
+    grid at steps 0 and 6, header in the documented BOV layout."""
+    g = np.load(os.path.join(GOLD, "bov_jacobi_24x20x16.npz"))
+    nz, ny, nx = (int(v) for v in g["shape"])
+    u0 = workloads.jacobi_initial(nx, ny, nz, seed=42)
+    for step in (0, int(g["steps"])):
+        data = np.frombuffer(bytes(g["data_%d" % step]), dtype=np.float64).reshape(nz, ny, nx)
+        np.testing.assert_array_equal(data, oracle.jacobi7(u0, step))
+        header = bytes(g["bov_%d" % step]).decode()
+        assert header.startswith("TIME: %d\nDATA_FILE: jac.%05d.data\nDATA_SIZE: %d %d %d\n" % (step, step, nx, ny, nz))
+        assert "DATA_FORMAT: DOUBLE\nVARIABLE: temp\n" in header
