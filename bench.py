@@ -174,8 +174,9 @@ class JacobiWorkload:
     def traffic_key(self):
         """Key of the committed ncu traffic line: the workload, plus _tb<d>
         when d > 1 steps are fused per pass (the library's default depth is
-        4 for the FP32 cell, 1 for the others)."""
-        depth = self.time_block or (4 if self.f32 else 1)
+        4 for the FP32 cell, 2 for the fixed-point cell)."""
+        depth = self.time_block or (4 if self.f32 else 2)
+        depth = depth if self.f32 else min(depth, 2)
         return self.name if depth <= 1 else "%s_tb%d" % (self.name, depth)
 
     def sync(self):
@@ -529,8 +530,8 @@ def run_gpu(args, world, rank, local, dist):
     if args.workload == "jacobi7_f64_512" and not args.no_ieee:
         # the same grid at the other blocking depths (steps fused per pass)
         sweep = {}
-        for depth in (1, 2, 3, 4):
-            if depth == (args.time_block or 1):
+        for depth in (1, 2):         # the fixed-point cell fuses at most two steps
+            if depth == min(args.time_block or 2, 2):     # the depth the headline ran at
                 continue
             w.set_time_block(depth)
             w.step(2 * depth)

@@ -60,13 +60,16 @@ int lgd_gpu_device_count(int *count);
  *                          bit-identical to the reference's SerialSimulator)
  *   LGD_CELL_JACOBI7_F64_FIX same cell with FP64 values at the ABI; on the
  *                          device the grid is held in 64-bit fixed point,
- *                          value = k * 2^(e - 59) with 2^e the smallest power
+ *                          value = k * 2^(e - 56) with 2^e the smallest power
  *                          of two above every value uploaded so far and the
  *                          edge cell.  The neighbour sum is exact and the
  *                          division by 7 rounds to the nearest unit, so each
- *                          step adds at most 2^(e - 60) absolute error.  For
- *                          GPUs whose FP64 pipe, not memory, would bound the
- *                          IEEE kernel.
+ *                          step adds at most 2^(e - 57) absolute error; a
+ *                          temporally blocked pass of two steps sums both
+ *                          exactly and rounds once (round of the exact
+ *                          two-step average, within one unit of two single
+ *                          steps).  For GPUs whose FP64 pipe, not memory,
+ *                          would bound the IEEE kernel.
  *   LGD_CELL_JACOBI7_F32   members {float temp}; same stencil in FP32
  *   LGD_CELL_SUM6_F64      members {double valA, double valB}; valB' = the
  *                          six face neighbours' valA summed in the order
@@ -220,12 +223,14 @@ int lgd_gpu_device_ptr(lgd_handle *h, int member, int which, void **ptr, size_t 
 int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count);
 
 /* Temporal blocking depth used by lgd_gpu_step (time steps fused into one
- * pass over memory): 0 = library default (4 for LGD_CELL_JACOBI7_F32, 1 for
- * the others), 1 = one step per pass, 2 .. LGD_TB_MAX_DEPTH.
- * Results are bit-identical for every depth.  It applies to the fixed-point
- * and FP32 Jacobi cells on 3D cube grids with a zero edge cell, under kernel
- * variants 0 and 6; a count of steps that is not a multiple of the depth
- * ends with one shorter pass.  Plays the role of the reference's
+ * pass over memory): 0 = library default (4 for LGD_CELL_JACOBI7_F32, 2 for
+ * LGD_CELL_JACOBI7_F64_FIX, 1 for the others), 1 = one step per pass,
+ * 2 .. LGD_TB_MAX_DEPTH.  It applies to the FP32 cell (results bit-identical
+ * for every depth) and the fixed-point cell (at most 2: its pass sums two
+ * steps exactly and rounds once; deeper requests run as passes of two) on
+ * 3D cube grids with a zero edge cell, under kernel variants 0 and 6; a
+ * count of steps that is not a multiple of the depth ends with one shorter
+ * pass.  Plays the role of the reference's
  * CacheBlockingSimulator pipelineLength, a wavefront of time steps over
  * z-marching frames (parallelization/cacheblockingsimulator.h:36-56); the
  * reference's CUDASimulator runs one step per launch

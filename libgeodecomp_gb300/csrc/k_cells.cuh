@@ -48,6 +48,20 @@ struct Jacobi7Fix {
     }
 };
 
+// Two Jacobi-7 steps in one pass with one rounding (the temporally blocked
+// fixed-point pass): the first level keeps the exact neighbour sum (7 times
+// the average), the second sums those and divides by 49.  The result is
+// round(exact two-step average), within one unit of two rounded single
+// steps.
+struct Jacobi7FixTwoStep {
+    typedef long long T;
+    static __device__ __forceinline__ T inner(T c, T n, T s, T e, T w, T t, T b) { return c + n + s + e + w + t + b; }
+    static __device__ __forceinline__ T last(T c, T n, T s, T e, T w, T t, T b)
+    {
+        return fx_div49_round(c + n + s + e + w + t + b);
+    }
+};
+
 // Variable-coefficient diffusion: u' = u + sum over faces (-x, +x, -y, +y,
 // -z, +z) of 0.5 (k + k_nb)(u_nb - u).
 template<typename R>

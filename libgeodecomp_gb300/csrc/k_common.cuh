@@ -60,21 +60,36 @@ __host__ __device__ __forceinline__ double splitmix_uniform(uint64_t key, uint64
 
 // ---- fixed-point representation of the FP64 Jacobi grid
 // value = k * 2^(scale_exp - LGD_FIX_BITS), k a signed 64-bit integer,
-// |value| < 2^scale_exp, so |k| < 2^59.  The averaging stencil maps
-// [-S, S] into itself, so 7 * 2^59 bounds every neighbour sum and nothing
-// overflows.
-#define LGD_FIX_BITS 59
+// |value| < 2^scale_exp, so |k| < 2^56.  The averaging stencil maps
+// [-S, S] into itself, so 7 * 2^56 bounds every neighbour sum, and 49 * 2^56
+// < 2^62 every exact two-step sum (the temporally blocked pass): nothing
+// overflows.  56 fraction bits: each rounding adds at most 2^(scale_exp - 57),
+// e.g. 6.9e-18 for values in [0, 1).
+#define LGD_FIX_BITS 56
 
 __device__ __forceinline__ long long fx_div7_round(long long sum)
 {
     // round(sum / 7) (no ties exist), via an unsigned offset so that the
-    // division is one multiply-high: for n < 7 * 2^60 + 3,
+    // division is one multiply-high: for n < 7 * 2^57 + 3 (and far beyond),
     // floor(n / 7) = floor(n * ceil(2^65 / 7) / 2^65) exactly (the error
-    // term n * (3/7) / 2^65 stays below 1/7).
-    const unsigned long long off = 7ull << 59;
+    // term n * (3/7) / 2^65 stays below 1/7)
+    const unsigned long long off = 7ull << LGD_FIX_BITS;
     const unsigned long long n = (unsigned long long)(sum + 3) + off;
     const unsigned long long q = __umul64hi(n, 0x4924924924924925ull) >> 1;
-    return (long long)(q - (1ull << 59));
+    return (long long)(q - (1ull << LGD_FIX_BITS));
+}
+
+__device__ __forceinline__ long long fx_div49_round(long long sum)
+{
+    // round(sum / 49) for |sum| < 49 * 2^56 (no ties: sum + 24 is never a
+    // multiple of 49 plus a half).  n = sum + 24 + 49 * 2^56 < 98 * 2^56 + 25;
+    // floor(n / 49) = floor(n * M / 2^69), M = ceil(2^69 / 49): with
+    // M * 49 - 2^69 = 34, the error term n * 34 / (49 * 2^69) stays below
+    // 1/49 for n < 2^69 / 34
+    const unsigned long long off = 49ull << LGD_FIX_BITS;
+    const unsigned long long n = (unsigned long long)(sum + 24) + off;
+    const unsigned long long q = __umul64hi(n, 0xa72f05397829cbc2ull) >> 5;
+    return (long long)(q - (1ull << LGD_FIX_BITS));
 }
 
 }  // namespace lgd

@@ -8,6 +8,8 @@
 // the halo re-reads, which hit L2.  Algorithmic traffic: one read and one
 // write per cell and step (16 B/cell for FP64, 8 B for FP32; varcoef adds
 // the coefficient read).
+#include <algorithm>
+
 #include "lgd_internal.h"
 #include "k_cells.cuh"
 
@@ -502,7 +504,8 @@ void launch_jacobi7(Grid& g, int steps)
     if ((g.variant == 0 || g.variant == 6) && tma_applicable(g)) {
         // temporal blocking: passes of `depth` steps, then one shorter pass
         // for the remainder (single steps go through the one-step kernel)
-        const int depth = (g.time_block == 0) ? (tb_applicable(g) ? tb_default_depth(g) : 1) : g.time_block;
+        int depth = (g.time_block == 0) ? (tb_applicable(g) ? tb_default_depth(g) : 1) : g.time_block;
+        if (tb_applicable(g)) depth = std::min(depth, tb_max_depth(g));
         if (depth > 1 && tb_applicable(g)) {
             while (steps >= 2) {
                 const int d = steps >= depth ? depth : steps;

@@ -1,4 +1,6 @@
 // Jacobi-7 with temporal blocking: TB time steps per pass over memory.
+// (The fixed-point cell's pass of two keeps exact neighbour sums at its
+// first level and rounds once at the second; see Jacobi7FixTwoStep.)
 //
 // A CTA owns a box of 64 x BH cells of every z plane of its z chunk and
 // marches in z.  One thread streams the box's input planes into a ring of
@@ -62,6 +64,27 @@ struct Geo {
     static constexpr int SMEM = (S + 2 * (TB - 1)) * PLANE;
     static_assert(OX > 0 && OY > 0, "box too small for the blocking depth");
     static_assert((OX * (int)sizeof(T)) % 16 == 0, "tile origins must stay 16-byte aligned");
+};
+
+// The rule a level applies: the cell's own rule at every level, except for
+// the two-step fixed-point cell, whose first level keeps exact sums and
+// whose last level rounds once
+template<typename CELL>
+struct TBOps {
+    typedef typename CELL::T T;
+    static __device__ __forceinline__ T level(bool last, T c, T n, T s, T e, T w, T t, T b)
+    {
+        return CELL::apply(c, n, s, e, w, t, b);
+    }
+};
+
+template<>
+struct TBOps<Jacobi7FixTwoStep> {
+    typedef long long T;
+    static __device__ __forceinline__ T level(bool last, T c, T n, T s, T e, T w, T t, T b)
+    {
+        return last ? Jacobi7FixTwoStep::last(c, n, s, e, w, t, b) : Jacobi7FixTwoStep::inner(c, n, s, e, w, t, b);
+    }
 };
 
 template<typename CELL, int TB, int WY, int ROWS>
@@ -157,8 +180,8 @@ jacobi7_tb_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T *
                 const T s1 = (r == ROWS - 1) ? sr1 : v[t - 1][PC][r + 1][1];
                 const T w0 = __shfl_up_sync(0xffffffffu, c1, 1);
                 const T e1 = __shfl_down_sync(0xffffffffu, c0, 1);
-                res[r][0] = CELL::apply(c0, n0, s0, c1, w0, v[t - 1][P][r][0], v[t - 1][PB][r][0]);
-                res[r][1] = CELL::apply(c1, n1, s1, e1, c0, v[t - 1][P][r][1], v[t - 1][PB][r][1]);
+                res[r][0] = TBOps<CELL>::level(t == TB, c0, n0, s0, c1, w0, v[t - 1][P][r][0], v[t - 1][PB][r][0]);
+                res[r][1] = TBOps<CELL>::level(t == TB, c1, n1, s1, e1, c0, v[t - 1][P][r][1], v[t - 1][PB][r][1]);
             }
             if (t < TB) {
                 // outside the grid an intermediate level keeps the edge value
@@ -304,43 +327,31 @@ bool tb_applicable(const Grid& g)
     }
 }
 
-// Default depth per cell, measured at 512^3 on GB300: the FP32 cell gains
-// 37% at depth 4; the fixed-point cell's integer arithmetic (about 40
-// instructions per update) makes a fused pass as slow as the passes it
-// replaces, so it keeps one step per pass (the single-step kernel runs at
-// 95% of HBM bandwidth).
+// Default depth per cell, measured at 512^3 on GB300: FP32 754 GLUPS at
+// depth 1, 1036 at depth 4; fixed point 403 at depth 1 (95% of HBM
+// bandwidth), 482 at depth 2 with exact two-step sums (a pass of two
+// single-rounding steps took as long as two HBM-bound single steps: the
+// per-step division by 7 costs a 64-bit multiply-high).
 int tb_default_depth(const Grid& g)
 {
-    return g.desc.cell == LGD_CELL_JACOBI7_F32 ? 4 : 1;
+    return g.desc.cell == LGD_CELL_JACOBI7_F32 ? 4 : 2;
 }
 
-// One pass of depth steps (2 .. LGD_TB_MAX_DEPTH) with box shape `shape`
-// (0 = the fastest measured on GB300 for the cell and depth; 1, 2 =
-// alternatives; warps x rows per warp; a shape that does not exist for a
-// depth runs shape 0):
-//   fixed point  depth 2: 16x4, 8x4, 16x2        depth 3: 16x2, 8x4
-//                depth 4: 16x2, 8x4
+// One pass of depth steps with box shape `shape` (0 = the fastest measured
+// on GB300 for the cell and depth; 1, 2 = alternatives; warps x rows per
+// warp; a shape that does not exist for a depth runs shape 0):
+//   fixed point  depth 2 (exact two-step sums, one rounding): 16x4, 8x4, 16x2
 //   FP32         depth 2, 3: 8x4                 depth 4: 16x4, 8x4, 16x2
-// Measured at 512^3 (GLUPS): fixed point 405 (depth 1), 406 / 328 / 340
-// (depth 2); FP32 754 (depth 1), 952 (depth 2), 870 (depth 3), 1036 / 949 /
-// 695 (depth 4).
 void launch_jacobi7_tb(Grid& g, int depth, int shape)
 {
     const int i64 = CU_TENSOR_MAP_DATA_TYPE_INT64;
     const int f32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
-        switch (depth * 10 + shape) {
-        case 21: launch_tb_typed<Jacobi7Fix, 2, 8, 4>(g, i64); break;
-        case 22: launch_tb_typed<Jacobi7Fix, 2, 16, 2>(g, i64); break;
-        case 31: launch_tb_typed<Jacobi7Fix, 3, 8, 4>(g, i64); break;
-        case 41: launch_tb_typed<Jacobi7Fix, 4, 8, 4>(g, i64); break;
-        default:
-            switch (depth) {
-            case 2: launch_tb_typed<Jacobi7Fix, 2, 16, 4>(g, i64); break;
-            case 3: launch_tb_typed<Jacobi7Fix, 3, 16, 2>(g, i64); break;
-            case 4: launch_tb_typed<Jacobi7Fix, 4, 16, 2>(g, i64); break;
-            default: throw Error(LGD_ERR_INVALID, "temporal blocking depth out of range");
-            }
+        LGD_REQUIRE(depth == 2, LGD_ERR_INVALID, "the fixed-point cell fuses two steps per pass");
+        switch (shape) {
+        case 1: launch_tb_typed<Jacobi7FixTwoStep, 2, 8, 4>(g, i64); break;
+        case 2: launch_tb_typed<Jacobi7FixTwoStep, 2, 16, 2>(g, i64); break;
+        default: launch_tb_typed<Jacobi7FixTwoStep, 2, 16, 4>(g, i64); break;
         }
     } else if (g.desc.cell == LGD_CELL_JACOBI7_F32) {
         switch (depth * 10 + shape) {
@@ -360,6 +371,13 @@ void launch_jacobi7_tb(Grid& g, int depth, int shape)
     check_launch("jacobi7 temporal blocking");
     ++g.launches;
     g.cur = 1 - g.cur;
+}
+
+// Deepest pass of a cell: the fixed-point cell's exact two-step sums stay
+// below 2^63 (49 * 2^56); deeper fusion would need fewer fraction bits.
+int tb_max_depth(const Grid& g)
+{
+    return g.desc.cell == LGD_CELL_JACOBI7_F64_FIX ? 2 : LGD_TB_MAX_DEPTH;
 }
 
 }  // namespace lgd

@@ -125,6 +125,7 @@ void launch_varcoef_tma(Grid& g);
 // temporal blocking (k_tb.cu): depth time steps per pass, 2 .. LGD_TB_MAX_DEPTH
 bool tb_applicable(const Grid& g);
 int tb_default_depth(const Grid& g);
+int tb_max_depth(const Grid& g);
 void launch_jacobi7_tb(Grid& g, int depth, int shape);
 
 // cuTensorMapEncodeTiled (tiled, no swizzle, no out-of-bounds NaN fill)
