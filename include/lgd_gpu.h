@@ -224,24 +224,29 @@ int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count);
 
 /* Temporal blocking depth used by lgd_gpu_step (time steps fused into one
  * pass over memory): 0 = library default (4 for LGD_CELL_JACOBI7_F32, 2 for
- * LGD_CELL_JACOBI7_F64_FIX, 1 for the others), 1 = one step per pass,
- * 2 .. LGD_TB_MAX_DEPTH.  It applies to the FP32 cell (results bit-identical
- * for every depth) and the fixed-point cell (at most 2: its pass sums two
- * steps exactly and rounds once; deeper requests run as passes of two) on
- * 3D cube grids with a zero edge cell, under kernel variants 0 and 6; a
- * count of steps that is not a multiple of the depth ends with one shorter
- * pass.  Plays the role of the reference's
- * CacheBlockingSimulator pipelineLength, a wavefront of time steps over
+ * LGD_CELL_JACOBI7_F64_FIX, 8 for LGD_CELL_GOL_U8, 1 for the others), 1 = one
+ * step per pass, 2 .. LGD_TB_MAX_DEPTH.  It applies to
+ *   - the FP32 Jacobi cell (at most 4; results bit-identical for every depth)
+ *     and the fixed-point Jacobi cell (at most 2: its pass sums two steps
+ *     exactly and rounds once) on 3D cube grids with a zero edge cell, under
+ *     kernel variants 0 and 6;
+ *   - Game of Life on a torus with rows of a multiple of 16 cells (depths
+ *     2, 4, 6, 8, 12; others run as the next smaller one; bit-identical),
+ *     under kernel variant 0.
+ * Deeper requests run at the cell's maximum; a count of steps that is not a
+ * multiple of the depth ends with shorter passes.  Plays the role of the
+ * reference's CacheBlockingSimulator pipelineLength, a wavefront of time steps over
  * z-marching frames (parallelization/cacheblockingsimulator.h:36-56); the
  * reference's CUDASimulator runs one step per launch
  * (parallelization/cudasimulator.h:560-594). */
-#define LGD_TB_MAX_DEPTH 4
+#define LGD_TB_MAX_DEPTH 12
 int lgd_gpu_set_time_block(lgd_handle *h, int depth);
 
 /* Box shape of the temporally blocked passes, for tuning and comparison:
- * 0 = the default for the cell and depth, 1 and 2 = alternatives (warps x
- * rows per warp; see k_tb.cu); a shape that does not exist for a depth runs
- * the default.  Results do not depend on the shape. */
+ * 0 = the default for the cell and depth, 1 and 2 = alternatives (Jacobi:
+ * warps x rows per warp, see k_tb.cu; Game of Life: strips twice as tall /
+ * half as tall); a shape that does not exist for a depth runs the default.
+ * Results do not depend on the shape. */
 int lgd_gpu_set_time_block_shape(lgd_handle *h, int shape);
 
 #ifdef __cplusplus

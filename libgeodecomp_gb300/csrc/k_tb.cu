@@ -373,11 +373,12 @@ void launch_jacobi7_tb(Grid& g, int depth, int shape)
     g.cur = 1 - g.cur;
 }
 
-// Deepest pass of a cell: the fixed-point cell's exact two-step sums stay
-// below 2^63 (49 * 2^56); deeper fusion would need fewer fraction bits.
+// Deepest Jacobi pass of a cell: the fixed-point cell's exact two-step sums
+// stay below 2^63 (49 * 2^56), deeper fusion would need fewer fraction bits;
+// the FP32 kernel is instantiated up to 4.
 int tb_max_depth(const Grid& g)
 {
-    return g.desc.cell == LGD_CELL_JACOBI7_F64_FIX ? 2 : LGD_TB_MAX_DEPTH;
+    return g.desc.cell == LGD_CELL_JACOBI7_F64_FIX ? 2 : 4;
 }
 
 }  // namespace lgd

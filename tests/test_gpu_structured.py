@@ -561,3 +561,56 @@ def test_temporal_blocking_default_depth_and_limits():
         g.step(8)
         assert g.launch_count() - before == 8
         np.testing.assert_array_equal(g.download(0), oracle.jacobi7(u0, 8))
+
+
+# ------------------------------------- Game of Life, generations per pass
+GOL_TB_GRIDS = [(16, 16), (32, 48), (40, 8192), (7, 64), (33, 480), (100, 496), (257, 1024), (3, 32)]
+
+
+def _gol_passes(steps, depth):
+    """Launches of the Game of Life path: passes of the largest compiled
+    depth (2, 4, 6, 8, 12) not above min(depth, steps left), single
+    generations for a remainder of one."""
+    n = 0
+    while steps >= 2:
+        d = max(k for k in (2, 4, 6, 8, 12) if k <= min(depth, steps))
+        steps -= d
+        n += 1
+    return n + steps
+
+
+@pytest.mark.parametrize("grid", GOL_TB_GRIDS)
+@pytest.mark.parametrize("depth", [2, 4, 6, 8, 12])
+def test_gol_generations_per_pass_bit_identical(grid, depth):
+    """Several generations per pass over memory (each warp marches down a
+    strip, generations skewed in registers, halo lanes wrapped around the
+    torus) give exactly the single-generation results: grids narrower than
+    a warp's 480 cells, shorter than the depth, wide ragged rows."""
+    c0 = workloads.gol_initial(grid[1], grid[0], seed=41)
+    steps = 2 * depth + 3
+    res = []
+    for d in (1, depth):
+        with lgd.Grid(lgd.CELL_GOL_U8, c0.shape, periodic=3) as g:
+            g.set_time_block(d)
+            g.upload(0, c0)
+            before = g.launch_count()
+            g.step(steps)
+            launches = g.launch_count() - before
+            res.append(g.download(0))
+        assert launches == (steps if d == 1 else _gol_passes(steps, d))
+    np.testing.assert_array_equal(res[1], res[0])
+    np.testing.assert_array_equal(res[0], oracle.gol(c0, steps))
+
+
+@pytest.mark.parametrize("shape", [1, 2])
+def test_gol_strip_shapes_identical(shape):
+    c0 = workloads.gol_initial(2048, 300, seed=43)
+    out = []
+    for s in (0, shape):
+        with lgd.Grid(lgd.CELL_GOL_U8, c0.shape, periodic=3) as g:
+            g.set_time_block(8)
+            g.set_time_block_shape(s)
+            g.upload(0, c0)
+            g.step(40)
+            out.append(g.download(0))
+    np.testing.assert_array_equal(out[0], out[1])
