@@ -104,8 +104,10 @@ int lgd_sell_launch_count(lgd_sell *h, uint64_t *count);
 
 /* Kernel variant (all give identical results): 0 = default, software
  * pipelined four slots deep (matrix entries of the next slots load while
- * the x gathers of the current ones are in flight); 1 = two slots per
- * iteration, no pipelining; 2 = pipelined two slots deep. */
+ * the x gathers of the current ones are in flight), CTAs of 128 threads;
+ * 1 = two slots per iteration, no pipelining, 256 threads; 2 = pipelined
+ * two slots deep, 256 threads; 3 = four deep, 64 threads; 4 = four deep,
+ * 256 threads; 5 = eight deep, 64 threads. */
 int lgd_sell_set_variant(lgd_sell *h, int variant);
 
 #ifdef __cplusplus

@@ -47,7 +47,7 @@ struct Sell {
     void *d_x[2];           // rows_padded each
     int *d_perm;            // physical -> logical (n), or null
     int cur;
-    int variant;            // 0 = pipelined (default), 1 = two gathers per iteration, 2 = pipelined depth 2
+    int variant;            // kernel variant, see lgd_sell_set_variant
     cudaStream_t stream;
     uint64_t launches;
 };
@@ -130,15 +130,12 @@ sell_diffusion_kernel(const int *__restrict__ chunk_offset, const int *__restric
 // every lane of the chunk, lanes load only their own row's entries; the
 // sum runs in slot order, as in the kernel above.
 template<typename R, bool EXACT, int D>
-__global__ void __launch_bounds__(256)
-sell_diffusion_pipe_kernel(const int *__restrict__ chunk_offset, const int *__restrict__ row_length,
-                           const R *__restrict__ values, const int *__restrict__ column,
-                           const R *__restrict__ x, R *__restrict__ xn, int n, int C, int row_begin, int row_end)
+__device__ __forceinline__ void sell_pipe_row(const int *__restrict__ chunk_offset, const int *__restrict__ row_length,
+                                              const R *__restrict__ values, const int *__restrict__ column,
+                                              const R *__restrict__ x, R *__restrict__ xn, int C, int row, int chunk)
 {
-    const int row = row_begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= row_end) return;
-    const int chunk = row / C;
-    const long long base = (long long)chunk_offset[chunk] + (row - chunk * C);
+    const long long cbase = chunk_offset[chunk];
+    const long long base = cbase + (row - chunk * C);
     const int len = row_length[row];
     const R xr = x[row];
     const R *v = values + base;
@@ -185,6 +182,25 @@ sell_diffusion_pipe_kernel(const int *__restrict__ chunk_offset, const int *__re
     }
 }
 
+// One thread per row.  The sigma-window sort puts a window's longest rows
+// into its first chunk, so the chunks (warps) of one CTA finish at very
+// different times and the CTA holds its slot until the longest is done;
+// CTAs of 128 threads (four chunks) measured 0.207 ms per step on the
+// 4M-node power-law matrix against 0.219 for 64 and 0.233 for 256 threads.
+// Loads stay on the read-only path: hints that skip L1 on the gathers,
+// keep x in L2 with evict_last or stream the matrix with evict_first, and
+// an L2 bulk prefetch of each chunk, all measured slower.
+template<typename R, bool EXACT, int D, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+sell_diffusion_pipe_kernel(const int *__restrict__ chunk_offset, const int *__restrict__ row_length,
+                           const R *__restrict__ values, const int *__restrict__ column,
+                           const R *__restrict__ x, R *__restrict__ xn, int n, int C, int row_begin, int row_end)
+{
+    const int row = row_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= row_end) return;
+    sell_pipe_row<R, EXACT, D>(chunk_offset, row_length, values, column, x, xn, C, row, row / C);
+}
+
 template<typename R>
 __global__ void permute_in_kernel(const double *logical, const int *perm, R *phys, int n)
 {
@@ -220,27 +236,33 @@ static void sell_free(Sell& s)
     if (s.stream) cudaStreamDestroy(s.stream);
 }
 
+template<typename R, bool EXACT, int D, int THREADS>
+static void launch_pipe(Sell& s, int row_begin, int row_end, const R *x, R *xn, const R *vals)
+{
+    const int blocks = (row_end - row_begin + THREADS - 1) / THREADS;
+    sell_diffusion_pipe_kernel<R, EXACT, D, THREADS><<<blocks, THREADS, 0, s.stream>>>(
+        s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
+}
+
 template<typename R, bool EXACT>
 static void launch_sell_typed(Sell& s, int row_begin, int row_end)
 {
-    const int threads = 256;
-    const int blocks = (row_end - row_begin + threads - 1) / threads;
     const R *x = (const R *)s.d_x[s.cur];
     R *xn = (R *)s.d_x[1 - s.cur];
     const R *vals = (const R *)s.d_values;
     switch (s.variant) {
-    case 1:
+    case 1: {
+        const int threads = 256;
+        const int blocks = (row_end - row_begin + threads - 1) / threads;
         sell_diffusion_kernel<R, EXACT><<<blocks, threads, 0, s.stream>>>(
             s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
         break;
-    case 2:
-        sell_diffusion_pipe_kernel<R, EXACT, 2><<<blocks, threads, 0, s.stream>>>(
-            s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
-        break;
-    default:
-        sell_diffusion_pipe_kernel<R, EXACT, 4><<<blocks, threads, 0, s.stream>>>(
-            s.d_chunk_offset, s.d_row_length, vals, s.d_column, x, xn, s.n, s.C, row_begin, row_end);
-        break;
+    }
+    case 2: launch_pipe<R, EXACT, 2, 256>(s, row_begin, row_end, x, xn, vals); break;
+    case 3: launch_pipe<R, EXACT, 4, 64>(s, row_begin, row_end, x, xn, vals); break;
+    case 4: launch_pipe<R, EXACT, 4, 256>(s, row_begin, row_end, x, xn, vals); break;
+    case 5: launch_pipe<R, EXACT, 8, 64>(s, row_begin, row_end, x, xn, vals); break;
+    default: launch_pipe<R, EXACT, 4, 128>(s, row_begin, row_end, x, xn, vals); break;
     }
 }
 
@@ -873,7 +895,7 @@ int lgd_sell_set_variant(lgd_sell *h, int variant)
 {
     return guard([&] {
         Sell& s = sell_of(h);
-        LGD_REQUIRE(variant >= 0 && variant <= 2, LGD_ERR_INVALID, "SELL kernel variant must lie in [0, 2]");
+        LGD_REQUIRE(variant >= 0 && variant <= 5, LGD_ERR_INVALID, "SELL kernel variant must lie in [0, 5]");
         s.variant = variant;
     });
 }

@@ -49,21 +49,21 @@ def test_sell_exact_bit_identical_to_reference():
     np.testing.assert_array_equal(out, g["out"])
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_sell_exact_every_kernel_variant_bit_identical(variant):
     g = load("sell_diffusion_2000")
     out, _, _ = gpu_run(2000, int(g["seed"]), int(g["steps"]), exact=True, variant=variant)
     np.testing.assert_array_equal(out, g["out"])
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_sell_fused_within_1e12_of_reference(variant):
     g = load("sell_diffusion_2000")
     out, _, _ = gpu_run(2000, int(g["seed"]), int(g["steps"]), variant=variant)
     assert rel_err(out, g["out"]) <= 1e-12
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_sell_ragged_rows_every_variant(variant):
     # rows of length 0 .. 9 (every residue of the pipeline depth), C = 8
     rng = np.random.default_rng(5)
