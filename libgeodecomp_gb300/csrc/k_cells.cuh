@@ -107,6 +107,26 @@ struct VarCoef<float> {
     }
 };
 
+// Two x-neighbouring FP32 cells (.x at x, .y at x + 1) in packed FP32
+// arithmetic (one instruction updates both, sm_100 and later):
+// u' = u + 0.5 * sum over faces (k + k_f)(u_f - u), each face's product
+// fused into the sum, faces in VarCoef's order.  One rounding fewer per
+// face than VarCoef<float>; both stay within the FP32 bound against the
+// FP64 cell.
+__device__ __forceinline__ float2 varcoef_pair_f32(float2 uc, float2 kc, float2 uw, float2 kw, float2 ue, float2 ke,
+                                                   float2 un, float2 kn, float2 us, float2 ks, float2 ub, float2 kb,
+                                                   float2 ut, float2 kt)
+{
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    float2 acc = __fmul2_rn(__fadd2_rn(kc, kw), __ffma2_rn(uc, m1, uw));
+    acc = __ffma2_rn(__fadd2_rn(kc, ke), __ffma2_rn(uc, m1, ue), acc);
+    acc = __ffma2_rn(__fadd2_rn(kc, kn), __ffma2_rn(uc, m1, un), acc);
+    acc = __ffma2_rn(__fadd2_rn(kc, ks), __ffma2_rn(uc, m1, us), acc);
+    acc = __ffma2_rn(__fadd2_rn(kc, kb), __ffma2_rn(uc, m1, ub), acc);
+    acc = __ffma2_rn(__fadd2_rn(kc, kt), __ffma2_rn(uc, m1, ut), acc);
+    return __ffma2_rn(make_float2(0.5f, 0.5f), acc, uc);
+}
+
 // Conway's rule (src/examples/gameoflife/main.cpp:35-58).
 __device__ __forceinline__ uint8_t gol_rule(uint8_t self, int living)
 {

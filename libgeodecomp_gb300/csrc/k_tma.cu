@@ -35,6 +35,16 @@ constexpr int ROWS = 4;
 constexpr int THREADS = 128;
 constexpr int D = 3;           // prefetch distance in planes
 constexpr int S = D + 2;       // ring slots: planes q-1, q, q+1 in use, D ahead
+// the var-coef kernel's ring (two fields per slot): prefetch distance and
+// slots, and whether FP32 pairs update in packed FP32 arithmetic.  Four
+// slots of 13.6 KB (FP32) leave room for four CTAs per SM; at 256^3 FP32
+// distance 2 measured 386 GLUPS against 368 for 3 (three CTAs per SM) and
+// 282 for 1, and the packed arithmetic 368 against 333 for scalar.  Carrying
+// the lane's own cells of planes z - 1 and z in registers (two shared loads
+// fewer per field and row, 87 registers) measured slower: 369.
+constexpr int VC_D = 2;
+constexpr int VC_S = VC_D + 2;
+constexpr bool VC_PACKED = true;
 
 template<typename T>
 struct Box {
@@ -205,7 +215,7 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
     typedef Box<R> B;
     typedef vc::Lay<R> Y;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[S];
+    __shared__ __align__(8) uint64_t bars[VC_S];
     __shared__ int s_fail;
     __shared__ int s_issued;
 
@@ -230,11 +240,11 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
                                            (need_w + need_e) * B::XPAD * B::H * sizeof(R));
 
     auto issue = [&](int q) {
-        const uint32_t bar = smem_addr(&bars[q % S]);
+        const uint32_t bar = smem_addr(&bars[q % VC_S]);
         int z = z0 - 1 + q;
         if (zw) z = (z + nz) % nz;
         mbar_expect_tx(bar, bytes);
-        unsigned char *slot = smem + (q % S) * Y::SLOT;
+        unsigned char *slot = smem + (q % VC_S) * Y::SLOT;
 #pragma unroll
         for (int f = 0; f < 2; ++f) {
             unsigned char *fb = slot + f * Y::FIELD;
@@ -247,10 +257,10 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
     };
 
     if (tid == 0) {
-        for (int s = 0; s < S; ++s) mbar_init(smem_addr(&bars[s]), 1);
+        for (int s = 0; s < VC_S; ++s) mbar_init(smem_addr(&bars[s]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_fail = 0;
-        const int first = min(D, nplanes - 1);
+        const int first = min(VC_D, nplanes - 1);
         for (int q = 0; q <= first; ++q) issue(q);
         s_issued = first + 1;
     }
@@ -258,7 +268,7 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
 
     int waited = -1;
     for (int q = 0; q < 2; ++q) {
-        if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1)) s_fail = 1;
+        if (!mbar_wait_bounded(smem_addr(&bars[q % VC_S]), (q / VC_S) & 1)) s_fail = 1;
         waited = q;
     }
 
@@ -274,19 +284,19 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
         const int q = z - z0 + 1;
         __syncthreads();
         if (s_fail) break;
-        if (tid == 0 && q + D < nplanes) {
-            issue(q + D);
-            s_issued = q + D + 1;
+        if (tid == 0 && q + VC_D < nplanes) {
+            issue(q + VC_D);
+            s_issued = q + VC_D + 1;
         }
-        if (!mbar_wait_bounded(smem_addr(&bars[(q + 1) % S]), ((q + 1) / S) & 1)) {
+        if (!mbar_wait_bounded(smem_addr(&bars[(q + 1) % VC_S]), ((q + 1) / VC_S) & 1)) {
             s_fail = 1;
             continue;
         }
         waited = q + 1;
 
-        const unsigned char *sb = smem + ((q - 1) % S) * Y::SLOT;
-        const unsigned char *sc = smem + (q % S) * Y::SLOT;
-        const unsigned char *st = smem + ((q + 1) % S) * Y::SLOT;
+        const unsigned char *sb = smem + ((q - 1) % VC_S) * Y::SLOT;
+        const unsigned char *sc = smem + (q % VC_S) * Y::SLOT;
+        const unsigned char *st = smem + ((q + 1) % VC_S) * Y::SLOT;
         R *orow = out + (long)z * plane + (long)(y0 + rw) * pitch + gx;
 #pragma unroll
         for (int j = 0; j < ROWS; ++j) {
@@ -320,7 +330,16 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
             }
             if (gx >= nx) continue;
             R *o = orow + (long)j * pitch;
-            if (gx + 1 < nx) {
+            if (VC_PACKED && sizeof(R) == 4 && gx + 1 < nx) {
+                // both cells in packed FP32 arithmetic
+                auto p2 = [](R a, R b) { return make_float2((float)a, (float)b); };
+                const float2 r2 = varcoef_pair_f32(
+                    p2(c[0][0], c[0][1]), p2(c[1][0], c[1][1]), p2(we[0], c[0][0]), p2(we[1], c[1][0]),
+                    p2(c[0][1], ea[0]), p2(c[1][1], ea[1]), p2(nb[0][0], nb[0][1]), p2(nb[1][0], nb[1][1]),
+                    p2(sb2[0][0], sb2[0][1]), p2(sb2[1][0], sb2[1][1]), p2(bt[0][0], bt[0][1]), p2(bt[1][0], bt[1][1]),
+                    p2(tp[0][0], tp[0][1]), p2(tp[1][0], tp[1][1]));
+                *reinterpret_cast<float2 *>(o) = r2;
+            } else if (gx + 1 < nx) {
                 const R o0 = VarCoef<R>::apply(c[0][0], c[1][0], we[0], we[1], c[0][1], c[1][1], nb[0][0], nb[1][0],
                                                sb2[0][0], sb2[1][0], bt[0][0], bt[1][0], tp[0][0], tp[1][0]);
                 const R o1 = VarCoef<R>::apply(c[0][1], c[1][1], c[0][0], c[1][0], ea[0], ea[1], nb[0][1], nb[1][1],
@@ -347,7 +366,7 @@ varcoef_tma_kernel(const __grid_constant__ vc::Maps maps, R *__restrict__ out, l
     if (s_fail) {
         if (tid == 0) atomicExch(err, 1);
         for (int q = waited + 1; q < s_issued; ++q) {
-            if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1)) break;
+            if (!mbar_wait_bounded(smem_addr(&bars[q % VC_S]), (q / VC_S) & 1)) break;
         }
     }
 }
@@ -533,7 +552,7 @@ static void launch_varcoef_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.vtmap_base[src][0] = ubuf;
         g.vtmap_base[src][1] = kbuf;
     }
-    const int smem = tmak::S * tmak::vc::Lay<R>::SLOT;
+    const int smem = tmak::VC_S * tmak::vc::Lay<R>::SLOT;
     static long long resident = 0;
     if (resident == 0) {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::varcoef_tma_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
