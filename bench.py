@@ -174,8 +174,8 @@ class JacobiWorkload:
     def traffic_key(self):
         """Key of the committed ncu traffic line: the workload, plus _tb<d>
         when d > 1 steps are fused per pass (the library's default depth is
-        4 for the FP32 cell, 2 for the fixed-point cell)."""
-        depth = self.time_block or (4 if self.f32 else 2)
+        3 for the FP32 cell, 2 for the fixed-point cell)."""
+        depth = self.time_block or (3 if self.f32 else 2)
         depth = depth if self.f32 else min(depth, 2)
         return self.name if depth <= 1 else "%s_tb%d" % (self.name, depth)
 

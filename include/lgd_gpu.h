@@ -223,7 +223,7 @@ int lgd_gpu_device_ptr(lgd_handle *h, int member, int which, void **ptr, size_t 
 int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count);
 
 /* Temporal blocking depth used by lgd_gpu_step (time steps fused into one
- * pass over memory): 0 = library default (4 for LGD_CELL_JACOBI7_F32, 2 for
+ * pass over memory): 0 = library default (3 for LGD_CELL_JACOBI7_F32, 2 for
  * LGD_CELL_JACOBI7_F64_FIX, 8 for LGD_CELL_GOL_U8, 1 for the others), 1 = one
  * step per pass, 2 .. LGD_TB_MAX_DEPTH.  It applies to
  *   - the FP32 Jacobi cell (at most 4; results bit-identical for every depth)

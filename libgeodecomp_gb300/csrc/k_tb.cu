@@ -76,6 +76,34 @@ struct TBOps {
     {
         return CELL::apply(c, n, s, e, w, t, b);
     }
+    // the lane's two x-neighbouring cells: (c0, n0, ...) and (c1, n1, ...)
+    static __device__ __forceinline__ void pair(bool last, T c0, T c1, T n0, T n1, T s0, T s1, T e0, T e1, T w0, T w1,
+                                                T t0, T t1, T b0, T b1, T& r0, T& r1)
+    {
+        r0 = level(last, c0, n0, s0, e0, w0, t0, b0);
+        r1 = level(last, c1, n1, s1, e1, w1, t1, b1);
+    }
+};
+
+// FP32 Jacobi-7 on both cells at once in packed FP32 arithmetic: the same
+// additions in the same order as Jacobi7F32::apply, each rounded to nearest,
+// so the results are bit-identical to the single-step kernels'.
+template<>
+struct TBOps<Jacobi7F32> {
+    typedef float T;
+    static __device__ __forceinline__ void pair(bool, T c0, T c1, T n0, T n1, T s0, T s1, T e0, T e1, T w0, T w1,
+                                                T t0, T t1, T b0, T b1, T& r0, T& r1)
+    {
+        float2 a = __fadd2_rn(make_float2(c0, c1), make_float2(n0, n1));
+        a = __fadd2_rn(a, make_float2(s0, s1));
+        a = __fadd2_rn(a, make_float2(e0, e1));
+        a = __fadd2_rn(a, make_float2(w0, w1));
+        a = __fadd2_rn(a, make_float2(t0, t1));
+        a = __fadd2_rn(a, make_float2(b0, b1));
+        a = __fmul2_rn(a, make_float2(1.0f / 7.0f, 1.0f / 7.0f));
+        r0 = a.x;
+        r1 = a.y;
+    }
 };
 
 template<>
@@ -84,6 +112,12 @@ struct TBOps<Jacobi7FixTwoStep> {
     static __device__ __forceinline__ T level(bool last, T c, T n, T s, T e, T w, T t, T b)
     {
         return last ? Jacobi7FixTwoStep::last(c, n, s, e, w, t, b) : Jacobi7FixTwoStep::inner(c, n, s, e, w, t, b);
+    }
+    static __device__ __forceinline__ void pair(bool last, T c0, T c1, T n0, T n1, T s0, T s1, T e0, T e1, T w0, T w1,
+                                                T t0, T t1, T b0, T b1, T& r0, T& r1)
+    {
+        r0 = level(last, c0, n0, s0, e0, w0, t0, b0);
+        r1 = level(last, c1, n1, s1, e1, w1, t1, b1);
     }
 };
 
@@ -180,8 +214,8 @@ jacobi7_tb_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T *
                 const T s1 = (r == ROWS - 1) ? sr1 : v[t - 1][PC][r + 1][1];
                 const T w0 = __shfl_up_sync(0xffffffffu, c1, 1);
                 const T e1 = __shfl_down_sync(0xffffffffu, c0, 1);
-                res[r][0] = TBOps<CELL>::level(t == TB, c0, n0, s0, c1, w0, v[t - 1][P][r][0], v[t - 1][PB][r][0]);
-                res[r][1] = TBOps<CELL>::level(t == TB, c1, n1, s1, e1, c0, v[t - 1][P][r][1], v[t - 1][PB][r][1]);
+                TBOps<CELL>::pair(t == TB, c0, c1, n0, n1, s0, s1, c1, e1, w0, c0, v[t - 1][P][r][0],
+                                  v[t - 1][P][r][1], v[t - 1][PB][r][0], v[t - 1][PB][r][1], res[r][0], res[r][1]);
             }
             if (t < TB) {
                 // outside the grid an intermediate level keeps the edge value
@@ -327,21 +361,23 @@ bool tb_applicable(const Grid& g)
     }
 }
 
-// Default depth per cell, measured at 512^3 on GB300: FP32 754 GLUPS at
-// depth 1, 1036 at depth 4; fixed point 403 at depth 1 (95% of HBM
+// Default depth per cell, measured at 512^3 on GB300: FP32 (packed pairs)
+// 754 GLUPS at depth 1, 932 at 2, 1100 at 3 (16x4), 1026 at 4; fixed point
+// 403 at depth 1 (95% of HBM
 // bandwidth), 482 at depth 2 with exact two-step sums (a pass of two
 // single-rounding steps took as long as two HBM-bound single steps: the
 // per-step division by 7 costs a 64-bit multiply-high).
 int tb_default_depth(const Grid& g)
 {
-    return g.desc.cell == LGD_CELL_JACOBI7_F32 ? 4 : 2;
+    return g.desc.cell == LGD_CELL_JACOBI7_F32 ? 3 : 2;
 }
 
 // One pass of depth steps with box shape `shape` (0 = the fastest measured
 // on GB300 for the cell and depth; 1, 2 = alternatives; warps x rows per
 // warp; a shape that does not exist for a depth runs shape 0):
 //   fixed point  depth 2 (exact two-step sums, one rounding): 16x4, 8x4, 16x2
-//   FP32         depth 2, 3: 8x4                 depth 4: 16x4, 8x4, 16x2
+//   FP32         depth 2: 8x4, 16x4, 16x2     depth 3: 16x4, 8x4, 16x2
+//                depth 4: 16x4, 8x4, 16x2
 void launch_jacobi7_tb(Grid& g, int depth, int shape)
 {
     const int i64 = CU_TENSOR_MAP_DATA_TYPE_INT64;
@@ -355,12 +391,16 @@ void launch_jacobi7_tb(Grid& g, int depth, int shape)
         }
     } else if (g.desc.cell == LGD_CELL_JACOBI7_F32) {
         switch (depth * 10 + shape) {
+        case 21: launch_tb_typed<Jacobi7F32, 2, 16, 4>(g, f32); break;
+        case 22: launch_tb_typed<Jacobi7F32, 2, 16, 2>(g, f32); break;
+        case 31: launch_tb_typed<Jacobi7F32, 3, 8, 4>(g, f32); break;
+        case 32: launch_tb_typed<Jacobi7F32, 3, 16, 2>(g, f32); break;
         case 41: launch_tb_typed<Jacobi7F32, 4, 8, 4>(g, f32); break;
         case 42: launch_tb_typed<Jacobi7F32, 4, 16, 2>(g, f32); break;
         default:
             switch (depth) {
             case 2: launch_tb_typed<Jacobi7F32, 2, 8, 4>(g, f32); break;
-            case 3: launch_tb_typed<Jacobi7F32, 3, 8, 4>(g, f32); break;
+            case 3: launch_tb_typed<Jacobi7F32, 3, 16, 4>(g, f32); break;
             case 4: launch_tb_typed<Jacobi7F32, 4, 16, 4>(g, f32); break;
             default: throw Error(LGD_ERR_INVALID, "temporal blocking depth out of range");
             }

@@ -503,7 +503,9 @@ def test_temporal_blocking_matches_single_steps(grid_shape, cell, depth):
 
 @pytest.mark.parametrize("cell,depth,shape", [(lgd.CELL_JACOBI7_F64_FIX, 2, 0), (lgd.CELL_JACOBI7_F64_FIX, 2, 1),
                                               (lgd.CELL_JACOBI7_F64_FIX, 2, 2), (lgd.CELL_JACOBI7_F32, 4, 1),
-                                              (lgd.CELL_JACOBI7_F32, 4, 2)])
+                                              (lgd.CELL_JACOBI7_F32, 4, 2), (lgd.CELL_JACOBI7_F32, 3, 1),
+                                              (lgd.CELL_JACOBI7_F32, 3, 2), (lgd.CELL_JACOBI7_F32, 2, 1),
+                                              (lgd.CELL_JACOBI7_F32, 2, 2)])
 @pytest.mark.parametrize("grid_shape", [(33, 61, 130), (70, 16, 64), (2, 1, 37), (12, 70, 250)])
 def test_temporal_blocking_box_shapes(cell, depth, shape, grid_shape):
     u0 = workloads.jacobi_initial(grid_shape[2], grid_shape[1], grid_shape[0], seed=29)
@@ -544,7 +546,7 @@ def test_temporal_blocking_default_depth_and_limits():
         g.upload(0, u0.astype(np.float32))
         before = g.launch_count()
         g.step(10)
-        assert g.launch_count() - before == 3          # FP32 default depth 4: 4 + 4 + 2
+        assert g.launch_count() - before == 4          # FP32 default depth 3: 3 + 3 + 3 + 1
     with lgd.Grid(lgd.CELL_JACOBI7_F64_FIX, u0.shape) as g:
         g.upload(0, u0)
         before = g.launch_count()
