@@ -757,7 +757,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=WORKLOAD_NAMES, default="jacobi7_f64_512")
-    ap.add_argument("--e2e-runs", type=int, default=2)
+    ap.add_argument("--e2e-runs", type=int, default=5)
     ap.add_argument("--size", type=int, default=512, help="cube edge of the Jacobi workloads (small profiling cases)")
     ap.add_argument("--time-block", type=int, default=0, help="Jacobi steps fused per pass (0 = library default)")
     ap.add_argument("--time-block-shape", type=int, default=0, help="box shape of the fused passes (tuning)")

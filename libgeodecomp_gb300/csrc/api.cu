@@ -178,6 +178,22 @@ static double *staging(Grid& g, size_t bytes)
     return (double *)g.d_stage;
 }
 
+// Row chunks of a fixed-point transfer: the copy of chunk k overlaps the
+// conversion of its neighbour (16 chunks: 64 MiB each at 512^3 FP64).
+constexpr int XFER_CHUNKS = 16;
+constexpr int ABSMAX_BLOCKS = 152;
+
+static void xfer_init(Grid& g)
+{
+    if (g.xfer_ready) return;
+    static_assert(XFER_CHUNKS + 1 <= (int)(sizeof(g.xfer_ev) / sizeof(g.xfer_ev[0])), "event array too small");
+    LGD_CHECK_CUDA(cudaStreamCreateWithFlags(&g.xfer_stream, cudaStreamNonBlocking));
+    for (int k = 0; k <= XFER_CHUNKS; ++k) {
+        LGD_CHECK_CUDA(cudaEventCreateWithFlags(&g.xfer_ev[k], cudaEventDisableTiming));
+    }
+    g.xfer_ready = true;
+}
+
 static Grid& grid_of(lgd_handle *h)
 {
     LGD_REQUIRE(h != nullptr, LGD_ERR_INVALID, "null handle");
@@ -345,6 +361,11 @@ int lgd_gpu_destroy(lgd_handle *h)
         if (g.d_partials) cudaFree(g.d_partials);
         if (g.d_err) cudaFree(g.d_err);
         if (g.d_stage) cudaFree(g.d_stage);
+        if (g.xfer_ready) {
+            cudaStreamSynchronize(g.xfer_stream);
+            for (int k = 0; k <= XFER_CHUNKS; ++k) cudaEventDestroy(g.xfer_ev[k]);
+            cudaStreamDestroy(g.xfer_stream);
+        }
         cudaStreamDestroy(g.stream);
         delete h;
     });
@@ -361,27 +382,51 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
         LGD_REQUIRE(bytes == n * helem, LGD_ERR_INVALID, "byte count does not match the grid");
         const size_t rows = (size_t)g.desc.ny * g.desc.nz;
         if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
-            // stage the doubles on the device, find max |value| there, then
-            // convert into the pitched fixed-point buffer
-            double *tmp = staging(g, n * 8 + 8 * 1024);
+            // Stage the doubles on the device in row chunks.  Each chunk is
+            // converted with the grid's current exponent as soon as it has
+            // landed, while the next one is copied, and its max |value| is
+            // kept per block.  If the maximum needs a larger exponent, the
+            // whole staging buffer is converted again after raising it.
+            const int K = (int)std::min<size_t>(XFER_CHUNKS, rows);
+            double *tmp = staging(g, n * 8 + 8 * (size_t)XFER_CHUNKS * ABSMAX_BLOCKS);
             double *partial = tmp + n;
-            LGD_CHECK_CUDA(cudaMemcpyAsync(tmp, host, n * 8, cudaMemcpyHostToDevice, g.stream));
-            absmax_kernel<<<1024, 256, 0, g.stream>>>(tmp, (long long)n, partial);
-            check_launch("max |value|");
-            ++g.launches;
-            double hpart[1024];
-            LGD_CHECK_CUDA(cudaMemcpyAsync(hpart, partial, sizeof(hpart), cudaMemcpyDeviceToHost, g.stream));
-            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
-            double m = std::fabs(g.desc.edge[0]);
-            for (int i = 0; i < 1024; ++i) m = std::fmax(m, hpart[i]);
-            LGD_REQUIRE(std::isfinite(m), LGD_ERR_INVALID, "grid holds a non-finite value");
-            raise_fix_exp(g, exp_bound(m));
             long long *dst = (long long *)member_buf(g, member, which);
             const size_t pitch = g.pitch_bytes[0] / 8;
-            to_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(tmp, dst, g.desc.nx, (long long)rows, (long long)pitch, g.fix_exp);
-            check_launch("to fixed point");
-            ++g.launches;
+            const size_t nx = (size_t)g.desc.nx;
+            const int e0 = g.fix_exp;
+            xfer_init(g);
+            // the copies wait for earlier work of the grid (the staging buffer)
+            LGD_CHECK_CUDA(cudaEventRecord(g.xfer_ev[XFER_CHUNKS], g.stream));
+            LGD_CHECK_CUDA(cudaStreamWaitEvent(g.xfer_stream, g.xfer_ev[XFER_CHUNKS], 0));
+            for (int k = 0; k < K; ++k) {
+                const size_t r0 = rows * k / K, r1 = rows * (k + 1) / K;
+                LGD_CHECK_CUDA(cudaMemcpyAsync(tmp + r0 * nx, (const double *)host + r0 * nx, (r1 - r0) * nx * 8,
+                                               cudaMemcpyHostToDevice, g.xfer_stream));
+                LGD_CHECK_CUDA(cudaEventRecord(g.xfer_ev[k], g.xfer_stream));
+                LGD_CHECK_CUDA(cudaStreamWaitEvent(g.stream, g.xfer_ev[k], 0));
+                absmax_kernel<<<ABSMAX_BLOCKS, 256, 0, g.stream>>>(tmp + r0 * nx, (long long)((r1 - r0) * nx),
+                                                                   partial + (size_t)k * ABSMAX_BLOCKS);
+                check_launch("max |value|");
+                to_fix_pitched_kernel<<<152 * 2, 256, 0, g.stream>>>(tmp + r0 * nx, dst + r0 * pitch, g.desc.nx,
+                                                                    (long long)(r1 - r0), (long long)pitch, e0);
+                check_launch("to fixed point");
+                g.launches += 2;
+            }
+            std::vector<double> hpart((size_t)K * ABSMAX_BLOCKS);
+            LGD_CHECK_CUDA(cudaMemcpyAsync(hpart.data(), partial, sizeof(double) * hpart.size(), cudaMemcpyDeviceToHost,
+                                           g.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            double m = std::fabs(g.desc.edge[0]);
+            for (double v : hpart) m = std::fmax(m, v);
+            LGD_REQUIRE(std::isfinite(m), LGD_ERR_INVALID, "grid holds a non-finite value");
+            if (exp_bound(m) > g.fix_exp) {
+                raise_fix_exp(g, exp_bound(m));
+                to_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(tmp, dst, g.desc.nx, (long long)rows,
+                                                                    (long long)pitch, g.fix_exp);
+                check_launch("to fixed point");
+                ++g.launches;
+                LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            }
             return;
         }
         LGD_CHECK_CUDA(cudaMemcpy2DAsync(member_buf(g, member, which), g.pitch_bytes[member], host,
@@ -402,13 +447,29 @@ int lgd_gpu_download(lgd_handle *h, int member, int which, void *host, size_t by
         LGD_REQUIRE(bytes == n * helem, LGD_ERR_INVALID, "byte count does not match the grid");
         const size_t rows = (size_t)g.desc.ny * g.desc.nz;
         if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
+            // convert row chunks on the grid's stream, copy each out on the
+            // transfer stream as soon as it is converted
+            const int K = (int)std::min<size_t>(XFER_CHUNKS, rows);
             double *tmp = staging(g, n * 8);
             const long long *src = (const long long *)member_buf(g, member, which);
             const size_t pitch = g.pitch_bytes[0] / 8;
-            from_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(src, tmp, g.desc.nx, (long long)rows, (long long)pitch, g.fix_exp);
-            check_launch("from fixed point");
-            ++g.launches;
-            LGD_CHECK_CUDA(cudaMemcpyAsync(host, tmp, n * 8, cudaMemcpyDeviceToHost, g.stream));
+            const size_t nx = (size_t)g.desc.nx;
+            xfer_init(g);
+            for (int k = 0; k < K; ++k) {
+                const size_t r0 = rows * k / K, r1 = rows * (k + 1) / K;
+                from_fix_pitched_kernel<<<152 * 2, 256, 0, g.stream>>>(src + r0 * pitch, tmp + r0 * nx, g.desc.nx,
+                                                                      (long long)(r1 - r0), (long long)pitch, g.fix_exp);
+                check_launch("from fixed point");
+                ++g.launches;
+                LGD_CHECK_CUDA(cudaEventRecord(g.xfer_ev[k], g.stream));
+                LGD_CHECK_CUDA(cudaStreamWaitEvent(g.xfer_stream, g.xfer_ev[k], 0));
+                LGD_CHECK_CUDA(cudaMemcpyAsync((double *)host + r0 * nx, tmp + r0 * nx, (r1 - r0) * nx * 8,
+                                               cudaMemcpyDeviceToHost, g.xfer_stream));
+            }
+            // later work of the grid (which may reuse the staging buffer)
+            // waits for the copies
+            LGD_CHECK_CUDA(cudaEventRecord(g.xfer_ev[XFER_CHUNKS], g.xfer_stream));
+            LGD_CHECK_CUDA(cudaStreamWaitEvent(g.stream, g.xfer_ev[XFER_CHUNKS], 0));
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
             check_device_error(g);
             return;

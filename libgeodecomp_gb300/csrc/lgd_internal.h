@@ -106,6 +106,12 @@ struct Grid {
     int *d_err;
     void *d_stage;          // conversion staging at the boundary (fixed-point grids)
     size_t stage_bytes;
+    // fixed-point transfers in row chunks: copies on xfer_stream, the
+    // conversions on stream, chunk k handed over by xfer_ev[k] (created on
+    // first use)
+    cudaStream_t xfer_stream;
+    cudaEvent_t xfer_ev[17];
+    bool xfer_ready;
     // var-coef TMA kernel: six tensor maps (u and k; main box, row, column)
     // per u buffer and the buffers they were built for
     alignas(64) unsigned char vtmap[2][6 * 128];
