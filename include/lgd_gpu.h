@@ -210,6 +210,24 @@ int lgd_sum_f64_static(const double *d_values, long long n, double *d_result, vo
  * their FP64 values.  Synchronises the handle's stream. */
 int lgd_gpu_write_bov(lgd_handle *h, int member, const char *prefix, unsigned step, const char *variable);
 
+/* Checkpoint snapshots in the file layout of the reference's MPIIOWriter /
+ * MPIIOInitializer (io/mpiio.h:85-125 writeRegion, :180-200 offsets;
+ * io/mpiiowriter.h, io/mpiioinitializer.h), written and read by one process
+ * without MPI: the dimensions as DIM 32-bit ints (x, y[, z]), the step and
+ * the maximum step count as 32-bit unsigned, the edge cell, then the cells
+ * x fastest.  A cell record is the grid's members in order in their host
+ * types, as the reference's sizeof(CELL) record for cells without padding;
+ * fixed-point grids hold FP64 values.
+ *   lgd_gpu_write_snapshot: writes the current grid (synchronises).
+ *   lgd_gpu_read_snapshot: loads a snapshot into the current grid; its
+ *     dimensions and edge cell must equal the grid's; returns the stored
+ *     step and maximum (either output may be null).
+ *   lgd_snapshot_info: the dimensions (dim entries), step and maximum of a
+ *     file, for restarting (startStep) before a grid exists. */
+int lgd_gpu_write_snapshot(lgd_handle *h, const char *path, unsigned step, unsigned max_steps);
+int lgd_gpu_read_snapshot(lgd_handle *h, const char *path, unsigned *step, unsigned *max_steps);
+int lgd_snapshot_info(const char *path, int dim, int *dims, unsigned *step, unsigned *max_steps);
+
 /* Sum of one member over the whole grid in FP64 (deterministic order). */
 int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum);
 

@@ -519,6 +519,131 @@ int lgd_gpu_write_bov(lgd_handle *h, int member, const char *prefix, unsigned st
     });
 }
 
+// Snapshot (checkpoint) files in the layout of the reference's MPIIO
+// (io/mpiio.h:85-125 writeRegion, :180-200 offset and getLengths): the
+// dimensions as DIM 32-bit ints (x, y[, z]), the step and the maximum step
+// count as 32-bit unsigned, the edge cell, then every cell at header +
+// index * cell bytes, index x fastest.  A cell record is the grid's members
+// in order, each in its host type (the reference writes sizeof(CELL)
+// bytes: the same for cells without padding).
+static size_t cell_record_bytes(const Grid& g)
+{
+    size_t b = 0;
+    for (int m = 0; m < g.n_members; ++m) b += (size_t)g.m[m].elem;
+    return b;
+}
+
+static void member_edge_bytes(const Grid& g, int m, unsigned char *out)
+{
+    const double e = g.desc.edge[m];
+    const int elem = g.m[m].elem;
+    if (elem == 8) {
+        std::memcpy(out, &e, 8);
+    } else if (elem == 4) {
+        const float f = (float)e;
+        std::memcpy(out, &f, 4);
+    } else {
+        out[0] = (unsigned char)(e != 0.0);
+    }
+}
+
+static std::vector<unsigned char> snapshot_header(const Grid& g, unsigned step, unsigned max_steps)
+{
+    const int dims[3] = {g.desc.nx, g.desc.ny, g.desc.nz};
+    std::vector<unsigned char> h(4 * (size_t)g.desc.dim + 8 + cell_record_bytes(g));
+    std::memcpy(h.data(), dims, 4 * (size_t)g.desc.dim);
+    std::memcpy(h.data() + 4 * g.desc.dim, &step, 4);
+    std::memcpy(h.data() + 4 * g.desc.dim + 4, &max_steps, 4);
+    size_t off = 4 * (size_t)g.desc.dim + 8;
+    for (int m = 0; m < g.n_members; ++m) {
+        member_edge_bytes(g, m, h.data() + off);
+        off += (size_t)g.m[m].elem;
+    }
+    return h;
+}
+
+int lgd_gpu_write_snapshot(lgd_handle *h, const char *path, unsigned step, unsigned max_steps)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(path != nullptr, LGD_ERR_INVALID, "null file name");
+        const size_t n = cells_of(g);
+        const size_t rec = cell_record_bytes(g);
+        std::vector<unsigned char> cells(n * rec);
+        size_t moff = 0;
+        for (int m = 0; m < g.n_members; ++m) {
+            const size_t elem = (size_t)g.m[m].elem;
+            std::vector<unsigned char> data(n * elem);
+            const int rc = lgd_gpu_download(h, m, 0, data.data(), data.size());
+            LGD_REQUIRE(rc == LGD_OK, rc, "download for the snapshot failed");
+            for (size_t i = 0; i < n; ++i) std::memcpy(&cells[i * rec + moff], &data[i * elem], elem);
+            moff += elem;
+        }
+        const std::vector<unsigned char> header = snapshot_header(g, step, max_steps);
+        FILE *f = std::fopen(path, "wb");
+        LGD_REQUIRE(f != nullptr, LGD_ERR_INVALID, std::string("cannot open ") + path);
+        const bool ok1 = std::fwrite(header.data(), 1, header.size(), f) == header.size();
+        const bool ok2 = std::fwrite(cells.data(), 1, cells.size(), f) == cells.size();
+        const bool ok3 = std::fclose(f) == 0;
+        LGD_REQUIRE(ok1 && ok2 && ok3, LGD_ERR_INVALID, std::string("cannot write ") + path);
+    });
+}
+
+int lgd_snapshot_info(const char *path, int dim, int *dims, unsigned *step, unsigned *max_steps)
+{
+    return guard([&] {
+        LGD_REQUIRE(path != nullptr && dims != nullptr && step != nullptr && max_steps != nullptr, LGD_ERR_INVALID,
+                    "null argument");
+        LGD_REQUIRE(dim == 2 || dim == 3, LGD_ERR_INVALID, "dim must be 2 or 3");
+        FILE *f = std::fopen(path, "rb");
+        LGD_REQUIRE(f != nullptr, LGD_ERR_INVALID, std::string("cannot open ") + path);
+        int d[3] = {0, 0, 1};
+        unsigned meta[2] = {0, 0};
+        const bool ok = std::fread(d, 4, (size_t)dim, f) == (size_t)dim && std::fread(meta, 4, 2, f) == 2;
+        std::fclose(f);
+        LGD_REQUIRE(ok, LGD_ERR_INVALID, std::string("snapshot header too short: ") + path);
+        for (int i = 0; i < dim; ++i) dims[i] = d[i];
+        *step = meta[0];
+        *max_steps = meta[1];
+    });
+}
+
+int lgd_gpu_read_snapshot(lgd_handle *h, const char *path, unsigned *step, unsigned *max_steps)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(path != nullptr, LGD_ERR_INVALID, "null file name");
+        const size_t n = cells_of(g);
+        const size_t rec = cell_record_bytes(g);
+        const std::vector<unsigned char> expect = snapshot_header(g, 0, 0);
+        std::vector<unsigned char> header(expect.size());
+        FILE *f = std::fopen(path, "rb");
+        LGD_REQUIRE(f != nullptr, LGD_ERR_INVALID, std::string("cannot open ") + path);
+        std::vector<unsigned char> cells(n * rec);
+        const bool ok1 = std::fread(header.data(), 1, header.size(), f) == header.size();
+        const bool ok2 = ok1 && std::fread(cells.data(), 1, cells.size(), f) == cells.size();
+        std::fclose(f);
+        LGD_REQUIRE(ok1, LGD_ERR_INVALID, std::string("snapshot header too short: ") + path);
+        const size_t dbytes = 4 * (size_t)g.desc.dim;
+        LGD_REQUIRE(std::memcmp(header.data(), expect.data(), dbytes) == 0, LGD_ERR_INVALID,
+                    "snapshot dimensions differ from the grid's");
+        LGD_REQUIRE(std::memcmp(header.data() + dbytes + 8, expect.data() + dbytes + 8, rec) == 0, LGD_ERR_INVALID,
+                    "snapshot edge cell differs from the grid's");
+        LGD_REQUIRE(ok2, LGD_ERR_INVALID, std::string("snapshot holds fewer cells than the grid: ") + path);
+        size_t moff = 0;
+        for (int m = 0; m < g.n_members; ++m) {
+            const size_t elem = (size_t)g.m[m].elem;
+            std::vector<unsigned char> data(n * elem);
+            for (size_t i = 0; i < n; ++i) std::memcpy(&data[i * elem], &cells[i * rec + moff], elem);
+            const int rc = lgd_gpu_upload(h, m, 0, data.data(), data.size());
+            LGD_REQUIRE(rc == LGD_OK, rc, "upload of the snapshot failed");
+            moff += elem;
+        }
+        if (step) std::memcpy(step, header.data() + dbytes, 4);
+        if (max_steps) std::memcpy(max_steps, header.data() + dbytes + 4, 4);
+    });
+}
+
 static void device_copy(lgd_handle *h, int member, int which, void *dev, size_t bytes, bool to_grid)
 {
     Grid& g = grid_of(h);

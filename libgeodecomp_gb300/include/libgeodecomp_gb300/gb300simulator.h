@@ -46,6 +46,7 @@
 #endif
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -470,6 +471,105 @@ private:
     GB300Simulator<CELL> *sim;
     int member;
     std::string variable;
+};
+
+// Checkpoints straight from the device grid of a GB300Simulator
+// (lgd_gpu_write_snapshot), in the file layout and under the file names of
+// the reference's MPIIOWriter (io/mpiiowriter.h: prefix + 5-digit step +
+// ".mpiio", written at WRITER_INITIALIZED, every period-th step and
+// WRITER_ALL_DONE; io/mpiio.h:85-125 for the layout), by one process
+// without MPI.  GB300SnapshotInitializer restarts from such a file.
+template<typename CELL>
+class GB300SnapshotWriter : public Writer<CELL> {
+public:
+    typedef typename Writer<CELL>::GridType GridType;
+
+    GB300SnapshotWriter(GB300Simulator<CELL> *sim, const std::string& prefix, unsigned period, unsigned maxSteps) :
+        Writer<CELL>(prefix, period), sim(sim), maxSteps(maxSteps)
+    {}
+
+    Writer<CELL> *clone() const { return new GB300SnapshotWriter(sim, this->prefix, this->period, maxSteps); }
+
+    void stepFinished(const GridType&, unsigned step, WriterEvent event)
+    {
+        if ((event == WRITER_STEP_FINISHED) && (step % this->period != 0)) return;
+        gb300Check(lgd_gpu_write_snapshot(sim->deviceHandle(), filename(step).c_str(), step, maxSteps));
+    }
+
+    std::string filename(unsigned step) const
+    {
+        char buf[16];
+        std::snprintf(buf, sizeof(buf), "%05u", step);
+        return this->prefix + buf + ".mpiio";
+    }
+
+private:
+    GB300Simulator<CELL> *sim;
+    unsigned maxSteps;
+};
+
+// Restart from a checkpoint: the reference's MPIIOInitializer
+// (io/mpiioinitializer.h) read by one process without MPI.  The
+// dimensions, start step and maximum come from the file's header, the grid
+// and its edge cell from the cell records (sizeof(CELL) bytes each, the
+// reference's record for cells without padding, at header + index *
+// sizeof(CELL), index x fastest; io/mpiio.h:28-66 readRegion).
+template<typename CELL>
+class GB300SnapshotInitializer : public Initializer<CELL> {
+public:
+    typedef typename Initializer<CELL>::Topology Topology;
+    static const int DIM = Topology::DIM;
+
+    explicit GB300SnapshotInitializer(const std::string& filename) :
+        file(filename)
+    {
+        int dims[3] = {1, 1, 1};
+        gb300Check(lgd_snapshot_info(file.c_str(), DIM, dims, &currentStep, &maximumSteps));
+        for (int d = 0; d < DIM; ++d) dimensions[d] = dims[d];
+    }
+
+    void grid(GridBase<CELL, DIM> *target)
+    {
+        const size_t header = 4 * DIM + 8;
+        const size_t cells = (size_t)dimensions.prod();
+        std::vector<unsigned char> bytes(header + (cells + 1) * sizeof(CELL));
+        FILE *f = std::fopen(file.c_str(), "rb");
+        if (!f) throw std::runtime_error("cannot open " + file);
+        const bool ok = std::fread(bytes.data(), 1, bytes.size(), f) == bytes.size();
+        std::fclose(f);
+        if (!ok) throw std::runtime_error("snapshot shorter than its header says: " + file);
+        CELL cell;
+        std::memcpy(static_cast<void *>(&cell), &bytes[header], sizeof(CELL));
+        target->setEdge(cell);
+        const unsigned char *data = &bytes[header + sizeof(CELL)];
+        const CoordBox<DIM> box = target->boundingBox();
+        for (size_t i = 0; i < cells; ++i) {
+            const Coord<DIM> c = coordOf(i);
+            if (!box.inBounds(c)) continue;
+            std::memcpy(static_cast<void *>(&cell), data + i * sizeof(CELL), sizeof(CELL));
+            target->set(c, cell);
+        }
+    }
+
+    Coord<DIM> gridDimensions() const { return dimensions; }
+    unsigned maxSteps() const { return maximumSteps; }
+    unsigned startStep() const { return currentStep; }
+
+private:
+    std::string file;
+    unsigned currentStep;
+    unsigned maximumSteps;
+    Coord<DIM> dimensions;
+
+    Coord<DIM> coordOf(size_t i) const
+    {
+        Coord<DIM> c;
+        for (int d = 0; d < DIM; ++d) {
+            c[d] = (int)(i % (size_t)dimensions[d]);
+            i /= (size_t)dimensions[d];
+        }
+        return c;
+    }
 };
 
 }  // namespace LibGeoDecomp

@@ -92,6 +92,9 @@ def lib():
             "lgd_gpu_set_time_block": [P, I],
             "lgd_gpu_set_time_block_shape": [P, I],
             "lgd_gpu_write_bov": [P, I, ctypes.c_char_p, ctypes.c_uint, ctypes.c_char_p],
+            "lgd_gpu_write_snapshot": [P, ctypes.c_char_p, ctypes.c_uint, ctypes.c_uint],
+            "lgd_gpu_read_snapshot": [P, ctypes.c_char_p, P, P],
+            "lgd_snapshot_info": [ctypes.c_char_p, I, P, P, P],
             "lgd_gpu_set_variant": [P, I],
             "lgd_gpu_stream": [P, P],
             "lgd_sell_plan": [I, P, I, I, P, P, P, P, P],
@@ -254,6 +257,17 @@ class Grid:
         """BOV snapshot of one member straight from the device (prefix.<step>.bov / .data)."""
         check(lib().lgd_gpu_write_bov(self._h, member, prefix.encode(), step, variable.encode()))
 
+    def write_snapshot(self, path: str, step: int, max_steps: int):
+        """Checkpoint of the current grid in the reference's MPIIO layout."""
+        check(lib().lgd_gpu_write_snapshot(self._h, path.encode(), step, max_steps))
+
+    def read_snapshot(self, path: str):
+        """Loads a checkpoint into the current grid; returns (step, max_steps)."""
+        step = ctypes.c_uint()
+        max_steps = ctypes.c_uint()
+        check(lib().lgd_gpu_read_snapshot(self._h, path.encode(), ctypes.byref(step), ctypes.byref(max_steps)))
+        return step.value, max_steps.value
+
     def set_time_block_shape(self, shape: int):
         check(lib().lgd_gpu_set_time_block_shape(self._h, shape))
 
@@ -269,6 +283,15 @@ class Grid:
 
 # ----------------------------------------------------------- SELL-C-sigma
 SELL_EXACT = 1
+
+
+def snapshot_info(path: str, dim: int = 3):
+    """(dims (x, y[, z]), step, max_steps) of a checkpoint file."""
+    dims = (ctypes.c_int * dim)()
+    step = ctypes.c_uint()
+    max_steps = ctypes.c_uint()
+    check(lib().lgd_snapshot_info(path.encode(), dim, dims, ctypes.byref(step), ctypes.byref(max_steps)))
+    return tuple(dims), step.value, max_steps.value
 
 
 def sell_build(n: int, row_ptr, col, w, C: int, sigma: int, remap_columns: bool = True) -> dict:

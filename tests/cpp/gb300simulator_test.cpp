@@ -305,6 +305,69 @@ static void testBovWriterFromDevice()
     }
 }
 
+// Checkpoints and restart, as the reference's MPIIOWriter / MPIIOInitializer
+// tests check them (io/test/parallel_mpi_1/mpiiowritertest.h,
+// io/test/parallel_mpi_2/mpiioinitializertest.h): files named prefix +
+// 5-digit step + ".mpiio" at steps 0, 4, ..., 20 and the last step 21, each
+// with its step and the maximum in the header and the grid of that step;
+// a simulation restarted from step 12 starts there and ends with the grid
+// of the uninterrupted run.
+static void testSnapshotWriterAndRestart()
+{
+    const Coord<3> dim(12, 9, 7);
+    const std::string prefix = "gb300_snapshot_test";
+    const std::size_t n = (std::size_t)dim.x() * dim.y() * dim.z();
+    {
+        GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 21));
+        GB300SnapshotWriter<JacobiCell> *writer = new GB300SnapshotWriter<JacobiCell>(&sim, prefix, 4, 21);
+        EXPECT(writer->filename(1234) == prefix + "01234.mpiio");
+        sim.addWriter(writer);
+        sim.run();
+    }
+    const unsigned at[7] = {0, 4, 8, 12, 16, 20, 21};
+    for (int k = 0; k < 7; ++k) {
+        char name[128];
+        std::snprintf(name, sizeof(name), "%s%05u.mpiio", prefix.c_str(), at[k]);
+        int dims[3] = {0, 0, 0};
+        unsigned step = 99, maxSteps = 99;
+        EXPECT(lgd_snapshot_info(name, 3, dims, &step, &maxSteps) == LGD_OK);
+        EXPECT(dims[0] == 12 && dims[1] == 9 && dims[2] == 7);
+        EXPECT(step == at[k] && maxSteps == 21);
+        // header: 3 ints, 2 unsigned, the edge cell; then the cells
+        std::vector<double> got(n + 1);
+        FILE *f = std::fopen(name, "rb");
+        EXPECT(f != nullptr);
+        if (!f) continue;
+        EXPECT(std::fseek(f, 20, SEEK_SET) == 0);
+        EXPECT(std::fread(got.data(), sizeof(double), n + 1, f) == n + 1);
+        EXPECT(std::fgetc(f) == EOF);
+        std::fclose(f);
+        EXPECT(got[0] == 0.25);
+        EXPECT(std::vector<double>(got.begin() + 1, got.end()) == cpuJacobi(dim, (int)at[k]));
+    }
+    {
+        GB300Simulator<JacobiCell> sim(new GB300SnapshotInitializer<JacobiCell>(prefix + "00012.mpiio"));
+        EXPECT(sim.getStep() == 12);
+        sim.run();
+        EXPECT(sim.getStep() == 21);
+        const GridBase<JacobiCell, 3> *grid = sim.getGrid();
+        const std::vector<double> expect = cpuJacobi(dim, 21);
+        bool same = true;
+        for (int z = 0; z < dim.z(); ++z)
+            for (int y = 0; y < dim.y(); ++y)
+                for (int x = 0; x < dim.x(); ++x) {
+                    same &= grid->get(Coord<3>(x, y, z)).temp == expect[((std::size_t)z * dim.y() + y) * dim.x() + x];
+                }
+        EXPECT(same);
+        EXPECT(grid->getEdge().temp == 0.25);
+    }
+    for (int k = 0; k < 7; ++k) {
+        char name[128];
+        std::snprintf(name, sizeof(name), "%s%05u.mpiio", prefix.c_str(), at[k]);
+        EXPECT(std::remove(name) == 0);
+    }
+}
+
 static void testBadBlockSizeThrows()
 {
     bool thrown = false;
@@ -380,6 +443,7 @@ int main()
     testBadBlockSizeThrows();
     testWriterReadsOnlyWhatItTouches();
     testBovWriterFromDevice();
+    testSnapshotWriterAndRestart();
     testGliderCrossesTorus();
     if (failures) {
         std::printf("%d failure(s)\n", failures);

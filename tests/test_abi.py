@@ -51,3 +51,20 @@ def test_create_reports_error_code_not_crash(library):
     assert e.value.code in (lgd.ERR_INVALID, lgd.ERR_CUDA)
     with pytest.raises(lgd.LGDError):
         lgd.Grid(999, (4, 4, 4))
+
+
+def test_snapshot_info_reads_the_reference_header(tmp_path):
+    """lgd_snapshot_info (host only) reads the header of the reference's
+    MPIIO layout (io/mpiio.h:70-79 readMetadata): DIM int32, step, maximum."""
+    import struct
+    from libgeodecomp_gb300 import lgd
+    p = tmp_path / "h00007.mpiio"
+    p.write_bytes(struct.pack("<3i2I", 12, 9, 7, 7, 21) + struct.pack("<d", 0.25) + bytes(8 * 12 * 9 * 7))
+    assert lgd.snapshot_info(str(p), 3) == ((12, 9, 7), 7, 21)
+    p2 = tmp_path / "h2.mpiio"
+    p2.write_bytes(struct.pack("<2i2I", 64, 40, 3, 5) + bytes(1 + 64 * 40))
+    assert lgd.snapshot_info(str(p2), 2) == ((64, 40), 3, 5)
+    p3 = tmp_path / "short.mpiio"
+    p3.write_bytes(struct.pack("<3i", 1, 2, 3))
+    with pytest.raises(lgd.LGDError):
+        lgd.snapshot_info(str(p3), 3)
