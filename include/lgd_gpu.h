@@ -81,6 +81,20 @@ int lgd_gpu_device_count(int *count);
  *   LGD_CELL_VARCOEF_F32 / _F64  members {u, k}; von Neumann r=1, 3D;
  *                          u' = u + sum_faces 0.5 (k + k_nb)(u_nb - u), faces
  *                          -x,+x,-y,+y,-z,+z; k' = k
+ *   LGD_CELL_TEST          one member, a 64-byte lgd_test_record; 1D, 2D or
+ *                          3D; the reference's self-validating TestCell
+ *                          (misc/testcell.h:205-372): every update checks
+ *                          each stencil neighbour as delivered (position
+ *                          wrapped by the topology, dimensions, cycle
+ *                          counter, edge-cell flag) and the nano step
+ *                          (== cycle % nano steps), then counts the cycle;
+ *                          any failed check clears `valid`.  desc.flags:
+ *                          LGD_TEST_VON_NEUMANN (else Moore r=1) |
+ *                          LGD_TEST_NANO_STEPS(n) (n in 1..255); edge[0] =
+ *                          the edge cell's valid flag + 2 * its edge flag.
+ *                          lgd_gpu_step's k-th update runs nano step
+ *                          (nano_step + k) % n.  For conformance tests of
+ *                          the simulator, not for speed.
  */
 #define LGD_CELL_JACOBI7_F64 1
 #define LGD_CELL_JACOBI7_F64_FIX 2
@@ -89,17 +103,32 @@ int lgd_gpu_device_count(int *count);
 #define LGD_CELL_GOL_U8 5
 #define LGD_CELL_VARCOEF_F32 6
 #define LGD_CELL_VARCOEF_F64 7
+#define LGD_CELL_TEST 8
+
+#define LGD_TEST_VON_NEUMANN 1
+#define LGD_TEST_NANO_STEPS(n) ((n) << 8)
+
+typedef struct lgd_test_record {
+    int32_t pos[3];         /* the cell's own idea of its position (unused axes 0) */
+    int32_t dim[3];         /* grid dimensions (unused axes 1) */
+    uint32_t cycle;         /* cycleCounter */
+    uint8_t edge;           /* isEdgeCell */
+    uint8_t valid;          /* isValid */
+    uint8_t pad0, pad1;
+    float test_value;       /* testValue, carried along */
+    int32_t pad[7];
+} lgd_test_record;
 
 /* periodic bit d set: axis d (0 = x, 1 = y, 2 = z) wraps (Topologies::Torus);
  * clear: cells outside read the constant edge cell (Topologies::Cube with
  * SoAGrid's edge cell, storage/soagrid.h:578-585, geometry/topologies.h:
  * 263-278). */
 typedef struct lgd_grid_desc {
-    int dim;            /* 2 or 3 */
-    int nx, ny, nz;     /* cells per axis; nz = 1 for 2D */
+    int dim;            /* 1, 2 or 3 (as the cell kind allows) */
+    int nx, ny, nz;     /* cells per axis; nz = 1 for 2D, ny = nz = 1 for 1D */
     int periodic;       /* bit mask, see above */
     int cell;           /* LGD_CELL_* */
-    int flags;          /* reserved, 0 */
+    int flags;          /* LGD_CELL_TEST: stencil and nano steps; else 0 */
     double edge[4];     /* edge cell, one value per member */
 } lgd_grid_desc;
 

@@ -45,6 +45,7 @@ static CellInfo cell_info(int cell)
     case LGD_CELL_GOL_U8:          return {1, {1, 0}, {1, 0}, {false, false}, 2, 2};
     case LGD_CELL_VARCOEF_F32:     return {2, {4, 4}, {4, 4}, {false, true}, 3, 3};
     case LGD_CELL_VARCOEF_F64:     return {2, {8, 8}, {8, 8}, {false, true}, 3, 3};
+    case LGD_CELL_TEST:            return {1, {64, 0}, {64, 0}, {false, false}, 1, 3};
     default:
         throw Error(LGD_ERR_INVALID, "unknown cell kind " + std::to_string(cell));
     }
@@ -300,6 +301,10 @@ int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
         LGD_REQUIRE(desc->dim >= ci.dim_min && desc->dim <= ci.dim_max, LGD_ERR_INVALID, "dimension does not match the cell");
         LGD_REQUIRE(desc->nx > 0 && desc->ny > 0 && desc->nz > 0, LGD_ERR_INVALID, "grid dimensions must be positive");
         LGD_REQUIRE(desc->dim == 3 || desc->nz == 1, LGD_ERR_INVALID, "2D grids have nz = 1");
+        LGD_REQUIRE(desc->dim >= 2 || desc->ny == 1, LGD_ERR_INVALID, "1D grids have ny = nz = 1");
+        LGD_REQUIRE(desc->cell == LGD_CELL_TEST ? (desc->flags & ~(LGD_TEST_VON_NEUMANN | 0xff00)) == 0
+                                                : desc->flags == 0,
+                    LGD_ERR_INVALID, "flags not defined for this cell kind");
         LGD_REQUIRE((desc->periodic & ~7) == 0, LGD_ERR_INVALID, "periodic mask has bits beyond z");
         int ndev = 0;
         LGD_CHECK_CUDA(cudaGetDeviceCount(&ndev));
@@ -490,6 +495,7 @@ int lgd_gpu_write_bov(lgd_handle *h, int member, const char *prefix, unsigned st
         LGD_REQUIRE(prefix != nullptr && variable != nullptr, LGD_ERR_INVALID, "null file prefix or variable name");
         const size_t n = cells_of(g);
         const int elem = g.m[member].elem;
+        LGD_REQUIRE(elem == 1 || elem == 4 || elem == 8, LGD_ERR_UNSUPPORTED, "BOV holds scalar members only");
         std::vector<unsigned char> data(n * elem);
         const int rc = lgd_gpu_download(h, member, 0, data.data(), data.size());
         LGD_REQUIRE(rc == LGD_OK, rc, "download for the BOV snapshot failed");
@@ -537,7 +543,21 @@ static void member_edge_bytes(const Grid& g, int m, unsigned char *out)
 {
     const double e = g.desc.edge[m];
     const int elem = g.m[m].elem;
-    if (elem == 8) {
+    if (g.desc.cell == LGD_CELL_TEST) {
+        // the reference TestInitializer's edge cell: position -1 on every
+        // axis, the grid's dimensions, cycle 0, test value 666
+        TestRec r;
+        std::memset(&r, 0, sizeof(r));
+        const int dims[3] = {g.desc.nx, g.desc.ny, g.desc.nz};
+        for (int a = 0; a < 3; ++a) {
+            r.pos[a] = a < g.desc.dim ? -1 : 0;
+            r.dim[a] = a < g.desc.dim ? dims[a] : 1;
+        }
+        r.valid = (unsigned char)((int)e & 1);
+        r.edge = (unsigned char)(((int)e >> 1) & 1);
+        r.test_value = 666.0f;
+        std::memcpy(out, &r, sizeof(r));
+    } else if (elem == 8) {
         std::memcpy(out, &e, 8);
     } else if (elem == 4) {
         const float f = (float)e;
@@ -713,7 +733,8 @@ int lgd_gpu_load_region(lgd_handle *h, int member, const int *streaks, int n_str
 
 int lgd_gpu_step(lgd_handle *h, unsigned nano_step, int count)
 {
-    (void)nano_step;   // the compiled cells have one nano step
+    // the compiled cells have one nano step, except the test cell, whose
+    // updates run nano steps nano_step, nano_step + 1, ...
     return guard([&] {
         Grid& g = grid_of(h);
         LGD_REQUIRE(count >= 0, LGD_ERR_INVALID, "negative step count");
@@ -746,7 +767,7 @@ int lgd_gpu_step(lgd_handle *h, unsigned nano_step, int count)
             const int n = (int)(streaks.size() / 4);
             const long long cells = stage_streaks(g, streaks.data(), n);
             for (int s = 0; s < count; ++s) {
-                launch_region(g, g.d_streaks, g.d_streak_prefix, n, cells);
+                launch_region(g, g.d_streaks, g.d_streak_prefix, n, cells, nano_step + (unsigned)s);
                 g.cur = 1 - g.cur;
             }
         }
@@ -756,11 +777,10 @@ int lgd_gpu_step(lgd_handle *h, unsigned nano_step, int count)
 
 int lgd_gpu_update_region(lgd_handle *h, const int *streaks, int n_streaks, unsigned nano_step)
 {
-    (void)nano_step;
     return guard([&] {
         Grid& g = grid_of(h);
         const long long cells = stage_streaks(g, streaks, n_streaks);
-        launch_region(g, g.d_streaks, g.d_streak_prefix, n_streaks, cells);
+        launch_region(g, g.d_streaks, g.d_streak_prefix, n_streaks, cells, nano_step);
     });
 }
 

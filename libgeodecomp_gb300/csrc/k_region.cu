@@ -94,6 +94,96 @@ __global__ void region_gol_kernel(View<const uint8_t> in, View<uint8_t> out, int
     out.at(x, y, z) = gol_rule(self, living - self);
 }
 
+// The self-validating test cell (LGD_CELL_TEST; the reference's TestCell,
+// misc/testcell.h:205-372): a cell copies itself, checks every neighbour of
+// its stencil as the simulator delivers it - the neighbour's position,
+// dimensions and cycle counter, and whether it is the edge cell, against
+// what the cell's own position and the topology imply - and the nano step
+// against its cycle counter, then counts the cycle.  A failed check clears
+// the valid flag (the cycle counter stays where it was when the nano step
+// is wrong, as in the reference).
+__device__ __forceinline__ bool test_check_neighbor(const TestRec& c, const TestRec& o, const int rel[3], int dim,
+                                                    int periodic)
+{
+    if (!o.valid) return false;
+    bool should_edge = false;
+    int expect[3] = {0, 0, 0};
+    for (int a = 0; a < dim; ++a) {
+        const int p = c.pos[a] + rel[a];
+        if ((periodic >> a) & 1) {
+            expect[a] = ((p % c.dim[a]) + c.dim[a]) % c.dim[a];
+        } else {
+            should_edge |= p < 0 || p >= c.dim[a];
+            expect[a] = p;
+        }
+    }
+    if ((o.edge != 0) != should_edge) return false;
+    if (!should_edge) {
+        if (o.cycle != c.cycle) return false;
+        for (int a = 0; a < dim; ++a) {
+            if (o.dim[a] != c.dim[a] || o.pos[a] != expect[a]) return false;
+        }
+    }
+    return true;
+}
+
+__global__ void region_test_kernel(View<const TestRec> in, View<TestRec> out, int dim, int periodic, int von_neumann,
+                                   unsigned nano_steps, unsigned nano, int edge_code, const int *streaks,
+                                   const long long *prefix, int n_streaks, long long cells)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= cells) return;
+    int x, y, z;
+    locate_cell(streaks, prefix, n_streaks, i, &x, &y, &z);
+    const TestRec c = in.at(x, y, z);
+    TestRec r = c;
+    if (c.edge) {
+        r.valid = 0;
+        out.at(x, y, z) = r;
+        return;
+    }
+    const int n[3] = {in.nx, in.ny, in.nz};
+    bool ok = c.valid != 0;
+    for (int dz = (dim > 2 ? -1 : 0); dz <= (dim > 2 ? 1 : 0); ++dz) {
+        for (int dy = (dim > 1 ? -1 : 0); dy <= (dim > 1 ? 1 : 0); ++dy) {
+            for (int dx = -1; dx <= 1; ++dx) {
+                if (von_neumann && abs(dx) + abs(dy) + abs(dz) > 1) continue;
+                const int rel[3] = {dx, dy, dz};
+                // the neighbour as delivered: wrapped on periodic axes, the
+                // edge cell beyond the others
+                int g[3] = {x + dx, y + dy, z + dz};
+                bool outside = false;
+                for (int a = 0; a < dim; ++a) {
+                    if (g[a] < 0 || g[a] >= n[a]) {
+                        if ((periodic >> a) & 1) {
+                            g[a] = (g[a] + n[a]) % n[a];
+                        } else {
+                            outside = true;
+                        }
+                    }
+                }
+                TestRec o;
+                if (outside) {
+                    o = TestRec();
+                    o.valid = (unsigned char)(edge_code & 1);
+                    o.edge = (unsigned char)((edge_code >> 1) & 1);
+                } else {
+                    o = in.at(g[0], g[1], g[2]);
+                }
+                ok &= test_check_neighbor(c, o, rel, dim, periodic);
+            }
+        }
+    }
+    if (nano >= nano_steps || nano != c.cycle % nano_steps) {
+        r.valid = 0;
+        out.at(x, y, z) = r;
+        return;
+    }
+    r.valid = ok ? 1 : 0;
+    r.cycle = c.cycle + 1;
+    out.at(x, y, z) = r;
+}
+
 template<typename R>
 __global__ void region_varcoef_kernel(View<const R> u, View<const R> k, View<R> out, int periodic, R edgeU, R edgeK,
                                       const int *streaks, const long long *prefix, int n_streaks, long long cells)
@@ -139,7 +229,8 @@ static View<const T> cview_of(Grid& g, int member, int which)
 
 long long fix_edge(const Grid& g);
 
-void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells)
+void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells,
+                   unsigned nano_step)
 {
     if (cells == 0) return;
     const int threads = 256;
@@ -176,6 +267,12 @@ void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int
         region_varcoef_kernel<double><<<(unsigned)blocks, threads, 0, g.stream>>>(
             cview_of<double>(g, 0, 0), cview_of<double>(g, 1, 0), view_of<double>(g, 0, 1), per,
             g.desc.edge[0], g.desc.edge[1], d_streaks, d_prefix, n_streaks, cells);
+        break;
+    case LGD_CELL_TEST:
+        region_test_kernel<<<(unsigned)blocks, threads, 0, g.stream>>>(
+            cview_of<TestRec>(g, 0, 0), view_of<TestRec>(g, 0, 1), g.desc.dim, per, g.desc.flags & LGD_TEST_VON_NEUMANN,
+            test_nano_steps(g), nano_step % test_nano_steps(g), (int)g.desc.edge[0], d_streaks, d_prefix, n_streaks,
+            cells);
         break;
     default:
         throw Error(LGD_ERR_UNSUPPORTED, "cell kind has no region kernel");
@@ -218,6 +315,10 @@ void launch_streak_copy(Grid& g, int member, int which, const int *d_streaks, co
     case 8:
         streak_copy_kernel<double><<<(unsigned)blocks, threads, 0, g.stream>>>(
             view_of<double>(g, member, which), d_streaks, d_prefix, n_streaks, cells, (double *)d_packed, to_grid);
+        break;
+    case 64:
+        streak_copy_kernel<TestRec><<<(unsigned)blocks, threads, 0, g.stream>>>(
+            view_of<TestRec>(g, member, which), d_streaks, d_prefix, n_streaks, cells, (TestRec *)d_packed, to_grid);
         break;
     default:
         throw Error(LGD_ERR_INVALID, "unsupported member size");

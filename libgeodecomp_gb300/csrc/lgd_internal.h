@@ -144,7 +144,25 @@ void encode_tensor_map(void *map, int dtype, int rank, void *base, const uint64_
 void launch_jacobi7(Grid& g, int steps);
 void launch_gol(Grid& g, int steps);
 void launch_varcoef(Grid& g, int steps);
-void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells);
+void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells,
+                   unsigned nano_step);
+
+// device form of lgd_test_record (LGD_CELL_TEST)
+struct TestRec {
+    int pos[3];
+    int dim[3];
+    unsigned cycle;
+    unsigned char edge, valid, pad0, pad1;
+    float test_value;
+    int pad[7];
+};
+static_assert(sizeof(TestRec) == 64, "test record is 64 bytes");
+
+inline unsigned test_nano_steps(const Grid& g)
+{
+    const unsigned n = ((unsigned)g.desc.flags >> 8) & 255u;
+    return n ? n : 1u;
+}
 void launch_fill(Grid& g, int member, int which, uint64_t seed, int stream, int mode, double p, int scale_exp);
 void launch_checksum(Grid& g, int member, int which, double *out);
 void launch_streak_copy(Grid& g, int member, int which, const int *d_streaks, const long long *d_prefix,

@@ -242,15 +242,29 @@ public:
 }  // namespace Topologies
 
 namespace Stencils {
+// lattice points with |x_1| + ... + |x_d| <= r, and (2 r + 1)^d
+constexpr int vonNeumannVolume(int d, int r)
+{
+    if (d == 0) return 1;
+    int n = 0;
+    for (int k = -r; k <= r; ++k) n += vonNeumannVolume(d - 1, r - (k < 0 ? -k : k));
+    return n;
+}
+constexpr int mooreVolume(int d, int r) { return d == 0 ? 1 : (2 * r + 1) * mooreVolume(d - 1, r); }
+
 template<int DIM, int RADIUS>
 class VonNeumann {
 public:
     static const int DIMENSIONS = DIM;
+    static const int RADIUS_ = RADIUS;
+    static const int VOLUME = vonNeumannVolume(DIM, RADIUS);
 };
 template<int DIM, int RADIUS>
 class Moore {
 public:
     static const int DIMENSIONS = DIM;
+    static const int RADIUS_ = RADIUS;
+    static const int VOLUME = mooreVolume(DIM, RADIUS);
 };
 }  // namespace Stencils
 
@@ -304,7 +318,20 @@ public:
     template<typename STENCIL>
     class HasStencil {
     public:
+        typedef void SupportsStencil;
         typedef STENCIL Stencil;
+    };
+
+    template<typename CELL, typename HAS = void>
+    class SelectStencil {
+    public:
+        typedef Stencils::Moore<2, 1> Value;
+    };
+
+    template<typename CELL>
+    class SelectStencil<CELL, typename CELL::API::SupportsStencil> {
+    public:
+        typedef typename CELL::API::Stencil Value;
     };
 
     class HasSoA {};

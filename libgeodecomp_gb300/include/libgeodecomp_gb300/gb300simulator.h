@@ -67,6 +67,76 @@ namespace LibGeoDecomp {
 template<typename CELL>
 class GB300CellTraits;
 
+// Optional in a binding: static int descFlags() - the grid descriptor's
+// flags (cell kinds that take some, LGD_CELL_TEST); 0 when absent.
+template<typename TRAITS>
+class GB300DescFlags {
+    template<typename U>
+    static char probe(decltype(&U::descFlags));
+    template<typename U>
+    static long probe(...);
+    template<typename U, bool HAS>
+    struct Get {
+        static int value() { return U::descFlags(); }
+    };
+    template<typename U>
+    struct Get<U, false> {
+        static int value() { return 0; }
+    };
+
+public:
+    static int value() { return Get<TRAITS, sizeof(probe<TRAITS>(0)) == 1>::value(); }
+};
+
+// Binding of a self-validating test cell to LGD_CELL_TEST: any class with
+// the members of the reference's TestCell (misc/testcell.h:159-164: pos,
+// dimensions, cycleCounter, isEdgeCell, isValid, testValue), its stencil
+// (Moore or von Neumann, radius 1) and NANO_STEPS.  Specialise
+// GB300CellTraits<TestCellType> by deriving from it.
+template<typename CELL>
+class GB300TestCellTraits {
+public:
+    typedef typename APITraits::SelectTopology<CELL>::Value Topology;
+    typedef typename APITraits::SelectStencil<CELL>::Value Stencil;
+    static const int DIM = Topology::DIM;
+    static const int KIND = LGD_CELL_TEST;
+    static const int MEMBERS = 1;
+    static std::size_t memberSize(int) { return sizeof(lgd_test_record); }
+    static int descFlags()
+    {
+        const bool vonNeumann = (DIM > 1) && (Stencil::VOLUME == 2 * DIM + 1);
+        return (vonNeumann ? LGD_TEST_VON_NEUMANN : 0) | LGD_TEST_NANO_STEPS((int)CELL::NANO_STEPS);
+    }
+    static void pack(const CELL& c, int, void *dst)
+    {
+        lgd_test_record r;
+        std::memset(&r, 0, sizeof(r));
+        for (int a = 0; a < 3; ++a) {
+            r.pos[a] = a < DIM ? c.pos[a] : 0;
+            r.dim[a] = a < DIM ? c.dimensions[a] : 1;
+        }
+        r.cycle = c.cycleCounter;
+        r.edge = c.isEdgeCell ? 1 : 0;
+        r.valid = c.isValid ? 1 : 0;
+        r.test_value = c.testValue;
+        std::memcpy(dst, &r, sizeof(r));
+    }
+    static void unpack(CELL *c, int, const void *src)
+    {
+        lgd_test_record r;
+        std::memcpy(&r, src, sizeof(r));
+        for (int a = 0; a < DIM; ++a) {
+            c->pos[a] = r.pos[a];
+            c->dimensions[a] = r.dim[a];
+        }
+        c->cycleCounter = r.cycle;
+        c->isEdgeCell = r.edge != 0;
+        c->isValid = r.valid != 0;
+        c->testValue = r.test_value;
+    }
+    static double edgeValue(const CELL& c, int) { return (c.isValid ? 1.0 : 0.0) + (c.isEdgeCell ? 2.0 : 0.0); }
+};
+
 // Maps a non-zero status of the C ABI to the exception the reference throws
 // in the same situation.
 inline void gb300Check(int rc)
@@ -341,6 +411,7 @@ private:
                      (Topology::template WrapsAxis<1>::VALUE ? 2 : 0) |
                      (Topology::template WrapsAxis<2>::VALUE ? 4 : 0);
         d.cell = Traits::KIND;
+        d.flags = GB300DescFlags<Traits>::value();
         for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
             d.edge[m] = Traits::edgeValue(hostGrid->getEdge(), m);
             edge[m] = d.edge[m];

@@ -29,6 +29,18 @@ CELL_SUM6_F64 = 4
 CELL_GOL_U8 = 5
 CELL_VARCOEF_F32 = 6
 CELL_VARCOEF_F64 = 7
+CELL_TEST = 8
+TEST_VON_NEUMANN = 1
+
+
+def TEST_NANO_STEPS(n: int) -> int:
+    return n << 8
+
+
+# lgd_test_record (include/lgd_gpu.h), 64 bytes
+TEST_RECORD = np.dtype([("pos", "<i4", 3), ("dim", "<i4", 3), ("cycle", "<u4"), ("edge", "u1"), ("valid", "u1"),
+                        ("pad0", "u1"), ("pad1", "u1"), ("test_value", "<f4"), ("pad", "<i4", 7)])
+assert TEST_RECORD.itemsize == 64
 
 # host dtype of each member, per cell kind
 MEMBERS = {
@@ -39,6 +51,7 @@ MEMBERS = {
     CELL_GOL_U8: [np.uint8],
     CELL_VARCOEF_F32: [np.float32, np.float32],
     CELL_VARCOEF_F64: [np.float64, np.float64],
+    CELL_TEST: [TEST_RECORD],
 }
 
 
@@ -155,9 +168,12 @@ def _ptr(a: np.ndarray):
 class Grid:
     """One structured device grid (a handle of the C ABI)."""
 
-    def __init__(self, cell: int, shape, periodic: int = 0, edge=(0.0, 0.0, 0.0, 0.0)):
+    def __init__(self, cell: int, shape, periodic: int = 0, edge=(0.0, 0.0, 0.0, 0.0), flags: int = 0):
         shape = tuple(int(s) for s in shape)
-        if len(shape) == 2:
+        if len(shape) == 1:
+            (nx,) = shape
+            ny, nz, dim = 1, 1, 1
+        elif len(shape) == 2:
             ny, nx = shape
             nz, dim = 1, 2
         else:
@@ -165,7 +181,7 @@ class Grid:
             dim = 3
         d = GridDesc()
         d.dim, d.nx, d.ny, d.nz = dim, nx, ny, nz
-        d.periodic, d.cell, d.flags = periodic, cell, 0
+        d.periodic, d.cell, d.flags = periodic, cell, flags
         for i, e in enumerate(list(edge)[:4]):
             d.edge[i] = float(e)
         self.cell = cell

@@ -11,6 +11,8 @@
 #include <libgeodecomp_gb300/gb300simulator.h>
 #ifdef LGD_GB300_WITH_REFERENCE
 #include <libgeodecomp/io/simpleinitializer.h>
+#include <libgeodecomp/io/testinitializer.h>
+#include <libgeodecomp/misc/testcell.h>
 #endif
 
 #include <cmath>
@@ -379,6 +381,178 @@ static void testBadBlockSizeThrows()
     EXPECT(thrown);
 }
 
+// ------------------------------------------- self-validating test cells
+// The conformance cases of the reference's CUDASimulator test
+// (parallelization/test/unit/cudasimulatortest.h:66-238): TestCell grids in
+// 1D, 2D and 3D, cube and torus, odd sizes, start steps other than 0 and
+// the block sizes of its multi-wavefront cases.  Every cell checks every
+// neighbour it is handed (position, dimensions, cycle, edge flag) and the
+// nano step on the device (LGD_CELL_TEST); the writer asserts the event
+// sequence and, at every call, that all cells are valid, none claims to be
+// the edge cell and all counted NANO_STEPS * step cycles
+// (io/testwriter.h:40-62, misc/testhelper.h:144-182).  Against the
+// reference's headers the cell and initializer are the reference's own
+// TestCell and TestInitializer; without them, restatements of both.
+#ifdef LGD_GB300_WITH_REFERENCE
+template<int DIM, typename STENCIL, typename TOPOLOGY>
+using GBTestCell = TestCell<DIM, STENCIL, TOPOLOGY, TestCellHelpers::EmptyAPI, TestCellHelpers::NoOutput>;
+template<typename CELL>
+using GBTestInitializer = TestInitializer<CELL>;
+#else
+template<int DIM, typename STENCIL, typename TOPOLOGY>
+class GBTestCell {
+public:
+    static const unsigned NANO_STEPS = DIM < 3 ? 27 : 3;
+    class API : public APITraits::HasTopology<TOPOLOGY>,
+                public APITraits::HasNanoSteps<NANO_STEPS>,
+                public APITraits::HasStencil<STENCIL> {};
+
+    GBTestCell() : cycleCounter(0), isEdgeCell(false), isValid(false), testValue(666) {}
+    GBTestCell(const Coord<DIM>& pos, const Coord<DIM>& dim, unsigned cycle = 0, float value = 666) :
+        pos(pos), dimensions(dim), cycleCounter(cycle), isEdgeCell(false), isValid(true), testValue(value)
+    {}
+    bool valid() const { return isValid; }
+    bool edgeCell() const { return isEdgeCell; }
+
+    Coord<DIM> pos;
+    Coord<DIM> dimensions;
+    unsigned cycleCounter;
+    bool isEdgeCell;
+    bool isValid;
+    float testValue;
+};
+
+template<typename CELL>
+class GBTestInitializer : public Initializer<CELL> {
+public:
+    typedef typename Initializer<CELL>::Topology Topology;
+    static const int DIM = Topology::DIM;
+
+    GBTestInitializer(const Coord<DIM>& dim, unsigned maxSteps, unsigned startStep = 0) :
+        dimensions(dim), maximumSteps(maxSteps), first(startStep)
+    {}
+
+    void grid(GridBase<CELL, DIM> *ret)
+    {
+        const CoordBox<DIM> box = ret->boundingBox();
+        const unsigned cycle = first * CELL::NANO_STEPS;
+        for (typename CoordBox<DIM>::Iterator i = box.begin(); i != box.end(); ++i) {
+            const Coord<DIM> c = Topology::normalize(*i, dimensions);
+            long index = 0;
+            for (int d = DIM - 1; d >= 0; --d) index = index * dimensions[d] + c[d];
+            ret->set(*i, CELL(c, dimensions, cycle, (float)(1 + index)));
+        }
+        Coord<DIM> minusOne;
+        for (int d = 0; d < DIM; ++d) minusOne[d] = -1;
+        CELL edgeCell(minusOne, dimensions);
+        edgeCell.isEdgeCell = true;
+        ret->setEdge(edgeCell);
+    }
+
+    Coord<DIM> gridDimensions() const { return dimensions; }
+    unsigned maxSteps() const { return maximumSteps; }
+    unsigned startStep() const { return first; }
+
+private:
+    Coord<DIM> dimensions;
+    unsigned maximumSteps;
+    unsigned first;
+};
+#endif
+
+typedef GBTestCell<1, Stencils::VonNeumann<1, 1>, Topologies::Cube<1>::Topology> TestCell1dCube;
+typedef GBTestCell<1, Stencils::Moore<1, 1>, Topologies::Torus<1>::Topology> TestCell1dTorus;
+typedef GBTestCell<2, Stencils::VonNeumann<2, 1>, Topologies::Cube<2>::Topology> TestCell2dCube;
+typedef GBTestCell<2, Stencils::Moore<2, 1>, Topologies::Torus<2>::Topology> TestCell2dTorus;
+typedef GBTestCell<3, Stencils::VonNeumann<3, 1>, Topologies::Cube<3>::Topology> TestCell3dCube;
+typedef GBTestCell<3, Stencils::Moore<3, 1>, Topologies::Torus<3>::Topology> TestCell3dTorus;
+
+namespace LibGeoDecomp {
+template<> class GB300CellTraits<TestCell1dCube> : public GB300TestCellTraits<TestCell1dCube> {};
+template<> class GB300CellTraits<TestCell1dTorus> : public GB300TestCellTraits<TestCell1dTorus> {};
+template<> class GB300CellTraits<TestCell2dCube> : public GB300TestCellTraits<TestCell2dCube> {};
+template<> class GB300CellTraits<TestCell2dTorus> : public GB300TestCellTraits<TestCell2dTorus> {};
+template<> class GB300CellTraits<TestCell3dCube> : public GB300TestCellTraits<TestCell3dCube> {};
+template<> class GB300CellTraits<TestCell3dTorus> : public GB300TestCellTraits<TestCell3dTorus> {};
+}
+
+template<typename CELL>
+class ConformanceWriter : public Writer<CELL> {
+public:
+    typedef typename Writer<CELL>::GridType GridType;
+    static const int DIM = APITraits::SelectTopology<CELL>::Value::DIM;
+
+    ConformanceWriter(unsigned period, unsigned firstStep, unsigned lastStep) :
+        Writer<CELL>("", period), bad(0)
+    {
+        steps.push_back(firstStep);
+        events.push_back(WRITER_INITIALIZED);
+        for (unsigned i = firstStep + period - firstStep % period; i < lastStep; i += period) {
+            steps.push_back(i);
+            events.push_back(WRITER_STEP_FINISHED);
+        }
+        steps.push_back(lastStep);
+        events.push_back(WRITER_ALL_DONE);
+    }
+
+    Writer<CELL> *clone() const { return new ConformanceWriter(*this); }
+
+    void stepFinished(const GridType& grid, unsigned step, WriterEvent event)
+    {
+        if (steps.empty()) {
+            ++bad;
+            return;
+        }
+        if (steps.front() != step || events.front() != event) ++bad;
+        steps.erase(steps.begin());
+        events.erase(events.begin());
+        const unsigned expectedCycle = CELL::NANO_STEPS * step;
+        if (!grid.getEdge().isEdgeCell || !grid.getEdge().isValid) ++bad;
+        const CoordBox<DIM> box = grid.boundingBox();
+        for (typename CoordBox<DIM>::Iterator i = box.begin(); i != box.end(); ++i) {
+            const CELL c = grid.get(*i);
+            if (!c.isValid || c.isEdgeCell || c.cycleCounter != expectedCycle) ++bad;
+        }
+    }
+
+    bool allEventsDone() const { return steps.empty() && events.empty(); }
+    long failures() const { return bad; }
+
+private:
+    std::vector<unsigned> steps;
+    std::vector<WriterEvent> events;
+    long bad;
+};
+
+template<typename CELL>
+static void runConformance(const Coord<APITraits::SelectTopology<CELL>::Value::DIM>& dim, unsigned startStep,
+                           unsigned endStep, unsigned period, Coord<3> blockSize = Coord<3>(128, 4, 1))
+{
+    GB300Simulator<CELL> sim(new GBTestInitializer<CELL>(dim, endStep, startStep), blockSize);
+    ConformanceWriter<CELL> *writer = new ConformanceWriter<CELL>(period, startStep, endStep);
+    sim.addWriter(writer);
+    sim.run();
+    EXPECT(writer->allEventsDone());
+    EXPECT(writer->failures() == 0);
+    EXPECT(sim.getStep() == endStep);
+}
+
+static void testTestCellConformance()
+{
+    runConformance<TestCell1dCube>(Coord<1>(777), 0, 33, 1);
+    runConformance<TestCell1dTorus>(Coord<1>(666), 40, 70, 3);
+    runConformance<TestCell2dCube>(Coord<2>(121, 151), 0, 21, 8);
+    runConformance<TestCell2dTorus>(Coord<2>(141, 131), 35, 60, 6);
+    runConformance<TestCell3dCube>(Coord<3>(50, 20, 10), 0, 5, 1);
+    runConformance<TestCell3dTorus>(Coord<3>(50, 20, 10), 28, 38, 3);
+    // the multiple-wavefront cases (block sizes are validated, the library
+    // picks its own launch shapes)
+    runConformance<TestCell2dCube>(Coord<2>(135, 127), 0, 21, 5, Coord<3>(128, 5, 1));
+    runConformance<TestCell2dTorus>(Coord<2>(251, 91), 0, 21, 6, Coord<3>(128, 5, 1));
+    runConformance<TestCell3dCube>(Coord<3>(52, 20, 14), 0, 6, 1, Coord<3>(128, 2, 3));
+    runConformance<TestCell3dTorus>(Coord<3>(54, 20, 13), 0, 7, 1, Coord<3>(64, 2, 3));
+}
+
 // ----------------------------------------------------- Game of Life (2D torus)
 class LifeCell {
 public:
@@ -445,6 +619,7 @@ int main()
     testBovWriterFromDevice();
     testSnapshotWriterAndRestart();
     testGliderCrossesTorus();
+    testTestCellConformance();
     if (failures) {
         std::printf("%d failure(s)\n", failures);
         return 1;
