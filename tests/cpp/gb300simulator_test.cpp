@@ -466,6 +466,17 @@ typedef GBTestCell<2, Stencils::VonNeumann<2, 1>, Topologies::Cube<2>::Topology>
 typedef GBTestCell<2, Stencils::Moore<2, 1>, Topologies::Torus<2>::Topology> TestCell2dTorus;
 typedef GBTestCell<3, Stencils::VonNeumann<3, 1>, Topologies::Cube<3>::Topology> TestCell3dCube;
 typedef GBTestCell<3, Stencils::Moore<3, 1>, Topologies::Torus<3>::Topology> TestCell3dTorus;
+// the SoA test cells (Moore, 3D), whose cases are fixme in the reference's
+// test (cudasimulatortest.h:211-239)
+#ifdef LGD_GB300_WITH_REFERENCE
+typedef TestCell<3, Stencils::Moore<3, 1>, Topologies::Cube<3>::Topology, TestCellHelpers::SoAAPI,
+                 TestCellHelpers::NoOutput> TestCellSoA3dCube;
+typedef TestCell<3, Stencils::Moore<3, 1>, Topologies::Torus<3>::Topology, TestCellHelpers::SoAAPI,
+                 TestCellHelpers::NoOutput> TestCellSoA3dTorus;
+#else
+typedef GBTestCell<3, Stencils::Moore<3, 1>, Topologies::Cube<3>::Topology> TestCellSoA3dCube;
+typedef TestCell3dTorus TestCellSoA3dTorus;
+#endif
 
 namespace LibGeoDecomp {
 template<> class GB300CellTraits<TestCell1dCube> : public GB300TestCellTraits<TestCell1dCube> {};
@@ -474,6 +485,10 @@ template<> class GB300CellTraits<TestCell2dCube> : public GB300TestCellTraits<Te
 template<> class GB300CellTraits<TestCell2dTorus> : public GB300TestCellTraits<TestCell2dTorus> {};
 template<> class GB300CellTraits<TestCell3dCube> : public GB300TestCellTraits<TestCell3dCube> {};
 template<> class GB300CellTraits<TestCell3dTorus> : public GB300TestCellTraits<TestCell3dTorus> {};
+template<> class GB300CellTraits<TestCellSoA3dCube> : public GB300TestCellTraits<TestCellSoA3dCube> {};
+#ifdef LGD_GB300_WITH_REFERENCE
+template<> class GB300CellTraits<TestCellSoA3dTorus> : public GB300TestCellTraits<TestCellSoA3dTorus> {};
+#endif
 }
 
 template<typename CELL>
@@ -551,6 +566,9 @@ static void testTestCellConformance()
     runConformance<TestCell2dTorus>(Coord<2>(251, 91), 0, 21, 6, Coord<3>(128, 5, 1));
     runConformance<TestCell3dCube>(Coord<3>(52, 20, 14), 0, 6, 1, Coord<3>(128, 2, 3));
     runConformance<TestCell3dTorus>(Coord<3>(54, 20, 13), 0, 7, 1, Coord<3>(64, 2, 3));
+    // the SoA cells, with the writer the reference's test leaves out
+    runConformance<TestCellSoA3dCube>(Coord<3>(54, 20, 13), 0, 7, 1, Coord<3>(64, 2, 3));
+    runConformance<TestCellSoA3dTorus>(Coord<3>(54, 20, 13), 0, 7, 1, Coord<3>(64, 2, 3));
 }
 
 // ----------------------------------------------------- Game of Life (2D torus)
