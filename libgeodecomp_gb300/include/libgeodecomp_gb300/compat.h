@@ -22,6 +22,8 @@
 #ifndef LGD_GB300_COMPAT_H
 #define LGD_GB300_COMPAT_H
 
+#include <algorithm>
+#include <chrono>
 #include <cstddef>
 #include <memory>
 #include <stdexcept>
@@ -496,8 +498,67 @@ protected:
     unsigned period;
 };
 
+// ------------------------------------------------------------ Chronometer
+// Accumulated wall time per category, with the reference's category ids
+// and names (misc/chronometer.h:142-150) and scoped timers that add the
+// time between their construction and destruction.
+class Chronometer {
+public:
+    static const std::size_t NUM_INTERVALS = 9;
+
+    Chronometer() : totalTimes(NUM_INTERVALS, 0.0) {}
+
+    double operator[](std::size_t i) const { return totalTimes[i]; }
+    double& operator[](std::size_t i) { return totalTimes[i]; }
+    double interval(std::size_t i) const { return totalTimes[i]; }
+    template<typename INTERVAL>
+    double interval() const { return totalTimes[INTERVAL::ID]; }
+    void reset() { std::fill(totalTimes.begin(), totalTimes.end(), 0.0); }
+
+    Chronometer& operator+=(const Chronometer& other)
+    {
+        for (std::size_t i = 0; i < NUM_INTERVALS; ++i) totalTimes[i] += other.totalTimes[i];
+        return *this;
+    }
+
+private:
+    std::vector<double> totalTimes;
+};
+
+namespace ChronometerHelpers {
+template<int EVENT_ID>
+class ScopedEvent {
+public:
+    static const int ID = EVENT_ID;
+    explicit ScopedEvent(Chronometer *chrono) : chrono(chrono), start(std::chrono::steady_clock::now()) {}
+    ~ScopedEvent()
+    {
+        (*chrono)[ID] += std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+    }
+
+private:
+    Chronometer *chrono;
+    std::chrono::steady_clock::time_point start;
+};
+}  // namespace ChronometerHelpers
+
+#define LGD_COMPAT_EVENT(NAME, EVENT_ID)                                                 \
+    class NAME : public ChronometerHelpers::ScopedEvent<EVENT_ID> {                     \
+    public:                                                                              \
+        explicit NAME(Chronometer *c) : ChronometerHelpers::ScopedEvent<EVENT_ID>(c) {}  \
+    };
+LGD_COMPAT_EVENT(TimeTotal, 0)
+LGD_COMPAT_EVENT(TimeCompute, 1)
+LGD_COMPAT_EVENT(TimeComputeInner, 2)
+LGD_COMPAT_EVENT(TimeComputeGhost, 3)
+LGD_COMPAT_EVENT(TimePatchAccepters, 4)
+LGD_COMPAT_EVENT(TimePatchProviders, 5)
+LGD_COMPAT_EVENT(TimeCommunication, 6)
+LGD_COMPAT_EVENT(TimeInput, 7)
+LGD_COMPAT_EVENT(TimeOutput, 8)
+#undef LGD_COMPAT_EVENT
+
 // -------------------------------------------------------------- Simulator
-class Chronometer {};
 
 template<typename CELL>
 class Simulator {

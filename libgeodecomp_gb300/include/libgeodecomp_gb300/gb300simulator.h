@@ -10,6 +10,9 @@
 // WRITER_STEP_FINISHED when step % period == 0 and WRITER_ALL_DONE at
 // maxSteps; SteererFeedback::endSimulation() stops run(); startStep() is
 // honoured.  The simulator owns the Initializer, Writers and Steerers.
+// gatherStatistics() reports SerialSimulator's chronometer categories
+// (total, compute, input, output; serialsimulator.h:78-164), compute time
+// including the device's (the reference's CUDASimulator leaves them 0).
 //
 // Differences from CUDASimulator, all on the host <-> device path:
 //   - Writers get a read-only view that copies planes of the grid to the
@@ -340,8 +343,13 @@ public:
     virtual void step(SteererFeedback *feedback)
     {
         handleInput(STEERER_NEXT_STEP, feedback);
-        for (unsigned i = 0; i < NANO_STEPS; ++i) {
-            gb300Check(lgd_gpu_step(handle, i, 1));
+        {
+            // compute time includes the device's: the scope waits for it
+            TimeCompute t(&this->chronometer);
+            for (unsigned i = 0; i < NANO_STEPS; ++i) {
+                gb300Check(lgd_gpu_step(handle, i, 1));
+            }
+            gb300Check(lgd_gpu_synchronize(handle));
         }
         view->invalidate();
         ++this->stepNum;
@@ -354,6 +362,7 @@ public:
 
     virtual void run()
     {
+        TimeTotal t(&this->chronometer);
         this->initializer->grid(hostGrid);
         view->markAllValid();
         this->stepNum = this->initializer->startStep();
@@ -486,13 +495,18 @@ private:
             next = std::min(next, (s + 1 + p - 1) / p * p - 1);        // (stepNum + 1) % p == 0
         }
         if (next <= s) return;
-        gb300Check(lgd_gpu_step(handle, 0, (int)std::min<unsigned>(next - s, 1u << 30)));
+        {
+            TimeCompute t(&this->chronometer);
+            gb300Check(lgd_gpu_step(handle, 0, (int)std::min<unsigned>(next - s, 1u << 30)));
+            gb300Check(lgd_gpu_synchronize(handle));
+        }
         this->stepNum = next;
         view->invalidate();
     }
 
     void handleInput(SteererEvent event, SteererFeedback *feedback)
     {
+        TimeInput t(&this->chronometer);
         bool called = false;
         for (std::size_t i = 0; i < this->steerers.size(); ++i) {
             if ((event != STEERER_NEXT_STEP) || (this->stepNum % this->steerers[i]->getPeriod() == 0)) {
@@ -507,6 +521,7 @@ private:
 
     void handleOutput(WriterEvent event)
     {
+        TimeOutput t(&this->chronometer);
         for (std::size_t i = 0; i < this->writers.size(); ++i) {
             if ((event != WRITER_STEP_FINISHED) || ((this->getStep() % this->writers[i]->getPeriod()) == 0)) {
                 this->writers[i]->stepFinished(*view, this->getStep(), event);   // planes on demand

@@ -370,6 +370,27 @@ static void testSnapshotWriterAndRestart()
     }
 }
 
+// gatherStatistics(): SerialSimulator's categories, filled - total time
+// covers compute, input and output, compute the device's work
+static void testStatistics()
+{
+    const Coord<3> dim(64, 48, 40);
+    std::vector<Event> log;
+    GB300Simulator<JacobiCell> sim(new JacobiInit(dim, 30));
+    sim.addWriter(new RecordingWriter(10, &log));
+    sim.run();
+    EXPECT(log.size() == 4);
+    const std::vector<Chronometer> stats = sim.gatherStatistics();
+    EXPECT(stats.size() == 1);
+    const Chronometer& c = stats[0];
+    EXPECT(c.interval<TimeTotal>() > 0);
+    EXPECT(c.interval<TimeCompute>() > 0);
+    EXPECT(c.interval<TimeOutput>() > 0);
+    EXPECT(c.interval<TimeInput>() >= 0);
+    EXPECT(c.interval<TimeCompute>() + c.interval<TimeInput>() + c.interval<TimeOutput>() <=
+           c.interval<TimeTotal>() * 1.001 + 1e-6);
+}
+
 static void testBadBlockSizeThrows()
 {
     bool thrown = false;
@@ -638,6 +659,7 @@ int main()
     testSnapshotWriterAndRestart();
     testGliderCrossesTorus();
     testTestCellConformance();
+    testStatistics();
     if (failures) {
         std::printf("%d failure(s)\n", failures);
         return 1;
