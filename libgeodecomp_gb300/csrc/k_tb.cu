@@ -174,6 +174,7 @@ jacobi7_tb_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T *
     const int rn = max(r0 - 1, 0);              // rim rows, clamped to the box (the clamped
     const int rs = min(r0 + ROWS, G::BH - 1);   // values only reach cells outside the tile)
     const bool xout = cx >= G::XP && cx < G::XP + G::OX && gx < nx;
+    const bool box_in = bx0 >= 0 && bx0 + BW <= nx && by0 >= 0 && by0 + G::BH <= ny;
     const long plane_elems = pitch * ny;
 
     T v[TB][3][ROWS][2];                        // level t's planes, rotating by i % 3
@@ -218,16 +219,27 @@ jacobi7_tb_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T *
                                   v[t - 1][P][r][1], v[t - 1][PB][r][0], v[t - 1][PB][r][1], res[r][0], res[r][1]);
             }
             if (t < TB) {
-                // outside the grid an intermediate level keeps the edge value
+                // outside the grid an intermediate level keeps the edge
+                // value; a plane of a box inside the grid needs no masks
+                // (the branch is uniform across the CTA)
                 const int gz = z0 - TB + i - t;
                 const bool zin = gz >= 0 && gz < nz;
                 unsigned char *dst = lvl + ((t - 1) * 2 + (i & 1)) * G::PLANE;
+                if (box_in && zin) {
 #pragma unroll
-                for (int r = 0; r < ROWS; ++r) {
-                    const bool yin = zin && ((ymask >> r) & 1u);
-                    v[t][P][r][0] = (yin && xin0) ? res[r][0] : T(0);
-                    v[t][P][r][1] = (yin && xin1) ? res[r][1] : T(0);
-                    st_pair<T>(dst + ((r0 + r) * BW + cx) * (int)sizeof(T), v[t][P][r][0], v[t][P][r][1]);
+                    for (int r = 0; r < ROWS; ++r) {
+                        v[t][P][r][0] = res[r][0];
+                        v[t][P][r][1] = res[r][1];
+                        st_pair<T>(dst + ((r0 + r) * BW + cx) * (int)sizeof(T), res[r][0], res[r][1]);
+                    }
+                } else {
+#pragma unroll
+                    for (int r = 0; r < ROWS; ++r) {
+                        const bool yin = zin && ((ymask >> r) & 1u);
+                        v[t][P][r][0] = (yin && xin0) ? res[r][0] : T(0);
+                        v[t][P][r][1] = (yin && xin1) ? res[r][1] : T(0);
+                        st_pair<T>(dst + ((r0 + r) * BW + cx) * (int)sizeof(T), v[t][P][r][0], v[t][P][r][1]);
+                    }
                 }
             } else if (xout) {
                 const int gz = z0 - 2 * TB + i;                 // in [z0, z1): level TB's plane
