@@ -229,10 +229,10 @@ class GoLWorkload:
     close = JacobiWorkload.close
 
     def set_time_block(self, depth, shape=0):
-        """Generations fused per pass (0 = the library's default, 8)."""
+        """Generations fused per pass (0 = the library's default, 16)."""
         self.g.set_time_block(depth)
         self.g.set_time_block_shape(shape)
-        self.config["generations_per_pass"] = "library default (8)" if depth == 0 else depth
+        self.config["generations_per_pass"] = "library default (16, bit-sliced)" if depth == 0 else depth
 
     def host_buffers(self, torch):
         hin = torch.empty(self.units, dtype=torch.uint8, pin_memory=True).numpy().reshape(self.shape)

@@ -271,22 +271,25 @@ int lgd_gpu_launch_count(lgd_handle *h, uint64_t *count);
 
 /* Temporal blocking depth used by lgd_gpu_step (time steps fused into one
  * pass over memory): 0 = library default (3 for LGD_CELL_JACOBI7_F32, 2 for
- * LGD_CELL_JACOBI7_F64_FIX, 8 for LGD_CELL_GOL_U8, 1 for the others), 1 = one
- * step per pass, 2 .. LGD_TB_MAX_DEPTH.  It applies to
+ * LGD_CELL_JACOBI7_F64_FIX, 16 for LGD_CELL_GOL_U8 with rows of a multiple
+ * of 32 cells, 8 for other Game of Life torus grids, 1 for the others),
+ * 1 = one step per pass, 2 .. LGD_TB_MAX_DEPTH.  It applies to
  *   - the FP32 Jacobi cell (at most 4; results bit-identical for every depth)
  *     and the fixed-point Jacobi cell (at most 2: its pass sums two steps
  *     exactly and rounds once) on 3D cube grids with a zero edge cell, under
  *     kernel variants 0 and 6;
- *   - Game of Life on a torus with rows of a multiple of 16 cells (depths
- *     2, 4, 6, 8, 12; others run as the next smaller one; bit-identical),
- *     under kernel variant 0.
+ *   - Game of Life on a torus (cells 0 or 1; bit-identical): rows of a
+ *     multiple of 32 cells run bit-sliced passes (32 cells per 32-bit word;
+ *     depths 2, 4, 6, 8, 12, 16, 24, 32) under kernel variant 0, rows of a
+ *     multiple of 16 cells byte passes (depths 2, 4, 6, 8, 12) under variant
+ *     0, or 1 to force them; other depths run as the next smaller one.
  * Deeper requests run at the cell's maximum; a count of steps that is not a
  * multiple of the depth ends with shorter passes.  Plays the role of the
  * reference's CacheBlockingSimulator pipelineLength, a wavefront of time steps over
  * z-marching frames (parallelization/cacheblockingsimulator.h:36-56); the
  * reference's CUDASimulator runs one step per launch
  * (parallelization/cudasimulator.h:560-594). */
-#define LGD_TB_MAX_DEPTH 12
+#define LGD_TB_MAX_DEPTH 32
 int lgd_gpu_set_time_block(lgd_handle *h, int depth);
 
 /* Box shape of the temporally blocked passes, for tuning and comparison:

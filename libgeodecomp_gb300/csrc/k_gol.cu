@@ -166,6 +166,129 @@ gol_tb_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int nx,
     }
 }
 
+// Bit-sliced temporal blocking (torus, nx a multiple of 32): a lane holds
+// 32 cells of a row as the bits of one 32-bit word (bit k = cell x0 + k),
+// a warp 32 words = 1024 cells, lanes 0 and 31 the wrapped halo words.  Per
+// generation and row, with a, m, c the rows above, at and below:
+//   column sums s = a + m + c as bit planes s0 = a ^ m ^ c, s1 = maj(a, m, c);
+//   the neighbour columns' sums by funnel shifts with the words of lanes
+//   l - 1 and l + 1 (four shuffles), and the 3 x 3 total, self included,
+//   T = sl + s + sr = u0 + 2 k with u0 = sl0 ^ s0 ^ sr0 and
+//   k = sl1 + s1 + sr1 + maj(sl0, s0, sr0) (0..4);
+//   next = (T == 3) | (m & T == 4) = (u0 & k == 1) | (~u0 & m & k == 2),
+// about twenty logic operations per 32 cells.  Rows arrive as bytes and
+// are packed with a multiply per 4 cells ((w * 0x10204080) >> 28 gathers
+// bytes 0..3 of w, each 0 or 1, into bits 0..3; no partial product reaches
+// bit 28 but the wanted ones), and stored back the same way
+// ((nibble * 0x00204081) & 0x01010101).  Wrong values spread one cell per
+// generation from a warp's halo words, so T <= 32 keeps lanes 1..30 exact.
+// The row march, prefetch and strips are those of gol_tb_kernel.
+__device__ __forceinline__ uint32_t gol_pack32(const uint4& lo, const uint4& hi)
+{
+    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    uint32_t r = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r |= ((w[i] * 0x10204080u) >> 28) << (4 * i);
+    return r;
+}
+
+__device__ __forceinline__ void gol_unpack32(uint32_t r, uint4& lo, uint4& hi)
+{
+    uint32_t w[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) w[i] = (((r >> (4 * i)) & 0xFu) * 0x00204081u) & 0x01010101u;
+    lo = make_uint4(w[0], w[1], w[2], w[3]);
+    hi = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
+__device__ __forceinline__ uint32_t gol_bits_row(uint32_t a, uint32_t m, uint32_t c)
+{
+    const uint32_t s0 = a ^ m ^ c;
+    const uint32_t s1 = (a & m) | (a & c) | (m & c);
+    const uint32_t s0l = __shfl_up_sync(0xffffffffu, s0, 1);
+    const uint32_t s1l = __shfl_up_sync(0xffffffffu, s1, 1);
+    const uint32_t s0r = __shfl_down_sync(0xffffffffu, s0, 1);
+    const uint32_t s1r = __shfl_down_sync(0xffffffffu, s1, 1);
+    const uint32_t x0 = __funnelshift_l(s0l, s0, 1);        // column x - 1
+    const uint32_t x1 = __funnelshift_l(s1l, s1, 1);
+    const uint32_t z0 = __funnelshift_r(s0, s0r, 1);        // column x + 1
+    const uint32_t z1 = __funnelshift_r(s1, s1r, 1);
+    const uint32_t u0 = x0 ^ s0 ^ z0;
+    const uint32_t c0 = (x0 & s0) | (x0 & z0) | (s0 & z0);
+    // k = x1 + s1 + z1 + c0 as two half sums a1 + 2 a2 and b1 + 2 b2
+    const uint32_t a1 = x1 ^ s1, a2 = x1 & s1;
+    const uint32_t b1 = z1 ^ c0, b2 = z1 & c0;
+    const uint32_t k1 = (a1 ^ b1) & ~(a2 | b2);
+    const uint32_t k2 = (a2 & ~(b1 | b2)) | (b2 & ~(a1 | a2)) | (a1 & b1);
+    return (u0 & k1) | (~u0 & m & k2);
+}
+
+template<int T>
+__global__ void __launch_bounds__(128)
+gol_bits_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int nx, int ny, long pitch, int strip,
+                int xwarps)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int xw = gw % xwarps;
+    const int y0 = (gw / xwarps) * strip;
+    if (y0 >= ny) return;                                   // warp-uniform
+    const int y1 = min(y0 + strip, ny);
+    const int nw = nx >> 5;
+    const int out_word = xw * 30 + lane - 1;
+    const int wd = ((out_word % nw) + nw) % nw;             // word this lane holds
+    const bool store = lane >= 1 && lane <= 30 && out_word < nw;
+    const int nrows = (y1 - y0) + 2 * T;                    // input row j is y0 - T + j
+    const uint8_t *col = in + (long)wd * 32;
+    auto row_of = [&](int j) { return ((y0 - T + j) % ny + ny) % ny; };
+    auto load = [&](int j, uint4& lo, uint4& hi) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(col + (long)row_of(j) * pitch);
+        lo = p[0];
+        hi = p[1];
+    };
+    auto put = [&](int j, uint32_t r) {                     // generation T's row j
+        const int y = y0 - T + j;                           // in [y0, y1)
+        uint4 lo, hi;
+        gol_unpack32(r, lo, hi);
+        uint4 *o = reinterpret_cast<uint4 *>(out + (long)y * pitch + (long)out_word * 32);
+        o[0] = lo;
+        o[1] = hi;
+    };
+
+    uint32_t v[T][3];
+    uint4 pl[3], ph[3];                                     // raw input rows: [j % 3] holds row j
+    load(0, pl[0], ph[0]);
+    if (nrows > 1) load(1, pl[1], ph[1]);
+
+    // generation t computes row i - t at iteration i from generation
+    // t - 1's rows of iterations i - 2 .. i
+    auto iteration = [&](auto phase, int i) {
+        constexpr int P = decltype(phase)::value;          // i % 3
+        constexpr int PC = (P + 2) % 3;                    // row i - 1 of a generation
+        constexpr int PB = (P + 1) % 3;                    // row i - 2
+        v[0][P] = gol_pack32(pl[P], ph[P]);
+        if (i + 2 < nrows) load(i + 2, pl[(P + 2) % 3], ph[(P + 2) % 3]);
+#pragma unroll
+        for (int t = 1; t <= T; ++t) {
+            if (i < 2 * t) break;                           // warp-uniform
+            const uint32_t r = gol_bits_row(v[t - 1][PB], v[t - 1][PC], v[t - 1][P]);
+            if (t < T) {
+                v[t][P] = r;
+            } else if (store) {
+                put(i - T, r);
+            }
+        }
+    };
+    for (int i = 0; i < nrows; i += 3) {
+        iteration(std::integral_constant<int, 0>(), i);
+        if (i + 1 < nrows) iteration(std::integral_constant<int, 1>(), i + 1);
+        if (i + 2 < nrows) iteration(std::integral_constant<int, 2>(), i + 2);
+    }
+}
+
+// generations per bit-sliced pass when none are requested
+constexpr int GOL_BITS_DEFAULT_DEPTH = 16;
+
 bool gol_tb_applicable(const Grid& g)
 {
     return g.desc.cell == LGD_CELL_GOL_U8 && (g.desc.periodic & 3) == 3 && g.desc.nz == 1 && g.desc.nx % 16 == 0 &&
@@ -203,6 +326,57 @@ static void launch_gol_tb_typed(Grid& g, int shape)
                                                                        (long)g.pitch_bytes[0], strip, xwarps);
 }
 
+bool gol_bits_applicable(const Grid& g)
+{
+    return gol_tb_applicable(g) && g.desc.nx % 32 == 0;
+}
+
+// one bit-sliced pass of `depth` generations (2, 4, 6, 8, 12, 16, 24, 32
+// instantiated; other depths run as the next smaller one); strips as for
+// the byte kernel, at least 4 * T rows
+template<int T>
+static void launch_gol_bits_typed(Grid& g, int shape)
+{
+    static int per_sm = 0;
+    static int sms = 0;
+    if (per_sm == 0) {
+        int dev = 0;
+        LGD_CHECK_CUDA(cudaGetDevice(&dev));
+        LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gol_bits_kernel<T>, 128, 0));
+        per_sm = std::max(1, per_sm);
+    }
+    const int nw = g.desc.nx / 32;
+    const int xwarps = (nw + 29) / 30;
+    const long long want = 1LL * sms * per_sm * 4;          // one wave of resident warps
+    int strip = (int)std::max<long long>(4 * T, ((long long)g.desc.ny * xwarps + want - 1) / want);
+    if (shape == 1) strip *= 2;
+    if (shape == 2) strip = std::max(2 * T, strip / 2);
+    strip = std::min(strip, g.desc.ny);
+    const long long warps = (long long)xwarps * ((g.desc.ny + strip - 1) / strip);
+    const uint8_t *in = (const uint8_t *)g.m[0].buf[g.cur];
+    uint8_t *out = (uint8_t *)g.m[0].buf[1 - g.cur];
+    gol_bits_kernel<T><<<(unsigned)((warps + 3) / 4), 128, 0, g.stream>>>(in, out, g.desc.nx, g.desc.ny,
+                                                                         (long)g.pitch_bytes[0], strip, xwarps);
+}
+
+static int gol_bits_pass(Grid& g, int depth, int shape)
+{
+    int d = 2;
+    if (depth >= 32) { launch_gol_bits_typed<32>(g, shape); d = 32; }
+    else if (depth >= 24) { launch_gol_bits_typed<24>(g, shape); d = 24; }
+    else if (depth >= 16) { launch_gol_bits_typed<16>(g, shape); d = 16; }
+    else if (depth >= 12) { launch_gol_bits_typed<12>(g, shape); d = 12; }
+    else if (depth >= 8) { launch_gol_bits_typed<8>(g, shape); d = 8; }
+    else if (depth >= 6) { launch_gol_bits_typed<6>(g, shape); d = 6; }
+    else if (depth >= 4) { launch_gol_bits_typed<4>(g, shape); d = 4; }
+    else { launch_gol_bits_typed<2>(g, shape); }
+    check_launch("game of life bit-sliced temporal blocking");
+    ++g.launches;
+    g.cur = 1 - g.cur;
+    return d;
+}
+
 static int gol_tb_pass(Grid& g, int depth, int shape)
 {
     int d = 0;
@@ -220,11 +394,20 @@ static int gol_tb_pass(Grid& g, int depth, int shape)
 void launch_gol(Grid& g, int steps)
 {
     LGD_REQUIRE(g.desc.nz == 1, LGD_ERR_INVALID, "Game of Life grids are 2D (nz = 1)");
-    // temporal blocking (torus, rows of a multiple of 16 cells): passes of
-    // `depth` generations, then single generations for a remainder of one
-    const int depth = (g.time_block == 0) ? 8 : std::min(g.time_block, 12);
-    if (g.variant == 0 && depth > 1 && gol_tb_applicable(g)) {
-        while (steps >= 2) steps -= gol_tb_pass(g, std::min(depth, steps), g.tb_shape);
+    // temporal blocking on the torus: bit-sliced passes (rows of a
+    // multiple of 32 cells, up to 32 generations) or byte passes (rows of a
+    // multiple of 16 cells, up to 12; variant 1 forces these for
+    // comparison), then single generations for a remainder of one
+    if (g.variant == 0 && gol_bits_applicable(g)) {
+        const int depth = (g.time_block == 0) ? GOL_BITS_DEFAULT_DEPTH : std::min(g.time_block, 32);
+        if (depth > 1) {
+            while (steps >= 2) steps -= gol_bits_pass(g, std::min(depth, steps), g.tb_shape);
+        }
+    } else if (g.variant <= 1 && gol_tb_applicable(g)) {
+        const int depth = (g.time_block == 0) ? 8 : std::min(g.time_block, 12);
+        if (depth > 1) {
+            while (steps >= 2) steps -= gol_tb_pass(g, std::min(depth, steps), g.tb_shape);
+        }
     }
 
     const bool swar = ((g.desc.periodic & 3) == 3) && (g.desc.nx % 16 == 0) && (g.pitch_bytes[0] % 16 == 0);

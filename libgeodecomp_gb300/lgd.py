@@ -20,7 +20,7 @@ ERR_CUDA = 3
 ERR_NOMEM = 4
 ERR_TIMEOUT = 5
 ERR_UNSUPPORTED = 6
-TB_MAX_DEPTH = 12       # LGD_TB_MAX_DEPTH
+TB_MAX_DEPTH = 32       # LGD_TB_MAX_DEPTH
 
 CELL_JACOBI7_F64 = 1
 CELL_JACOBI7_F64_FIX = 2

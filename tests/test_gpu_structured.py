@@ -569,37 +569,47 @@ def test_temporal_blocking_default_depth_and_limits():
 GOL_TB_GRIDS = [(16, 16), (32, 48), (40, 8192), (7, 64), (33, 480), (100, 496), (257, 1024), (3, 32)]
 
 
-def _gol_passes(steps, depth):
+GOL_BIT_DEPTHS = (2, 4, 6, 8, 12, 16, 24, 32)
+GOL_BYTE_DEPTHS = (2, 4, 6, 8, 12)
+
+
+def _gol_passes(steps, depth, nx, variant=0):
     """Launches of the Game of Life path: passes of the largest compiled
-    depth (2, 4, 6, 8, 12) not above min(depth, steps left), single
-    generations for a remainder of one."""
+    depth not above min(depth, steps left) - bit-sliced passes for rows of a
+    multiple of 32 cells, byte passes otherwise or under variant 1 - and
+    single generations for a remainder of one."""
+    depths = GOL_BIT_DEPTHS if (nx % 32 == 0 and variant == 0) else GOL_BYTE_DEPTHS
     n = 0
     while steps >= 2:
-        d = max(k for k in (2, 4, 6, 8, 12) if k <= min(depth, steps))
+        d = max(k for k in depths if k <= min(depth, steps))
         steps -= d
         n += 1
     return n + steps
 
 
 @pytest.mark.parametrize("grid", GOL_TB_GRIDS)
-@pytest.mark.parametrize("depth", [2, 4, 6, 8, 12])
-def test_gol_generations_per_pass_bit_identical(grid, depth):
+@pytest.mark.parametrize("depth,variant", [(2, 0), (4, 0), (6, 0), (8, 0), (12, 0), (16, 0), (24, 0), (32, 0),
+                                           (4, 1), (12, 1)])
+def test_gol_generations_per_pass_bit_identical(grid, depth, variant):
     """Several generations per pass over memory (each warp marches down a
-    strip, generations skewed in registers, halo lanes wrapped around the
-    torus) give exactly the single-generation results: grids narrower than
-    a warp's 480 cells, shorter than the depth, wide ragged rows."""
+    strip, generations skewed in registers, halo lanes or words wrapped
+    around the torus) give exactly the single-generation results: grids
+    narrower than a warp, shorter than the depth, wide ragged rows, in the
+    bit-sliced passes (rows of a multiple of 32 cells) and the byte passes
+    (variant 1, or rows of a multiple of 16)."""
     c0 = workloads.gol_initial(grid[1], grid[0], seed=41)
     steps = 2 * depth + 3
     res = []
     for d in (1, depth):
         with lgd.Grid(lgd.CELL_GOL_U8, c0.shape, periodic=3) as g:
             g.set_time_block(d)
+            g.set_variant(variant)
             g.upload(0, c0)
             before = g.launch_count()
             g.step(steps)
             launches = g.launch_count() - before
             res.append(g.download(0))
-        assert launches == (steps if d == 1 else _gol_passes(steps, d))
+        assert launches == (steps if d == 1 else _gol_passes(steps, d, grid[1], variant))
     np.testing.assert_array_equal(res[1], res[0])
     np.testing.assert_array_equal(res[0], oracle.gol(c0, steps))
 
