@@ -229,7 +229,7 @@ gol_bits_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int n
                 int xwarps)
 {
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int xw = gw % xwarps;
     const int y0 = (gw / xwarps) * strip;
     if (y0 >= ny) return;                                   // warp-uniform
@@ -337,18 +337,19 @@ bool gol_bits_applicable(const Grid& g)
 template<int T>
 static void launch_gol_bits_typed(Grid& g, int shape)
 {
+    constexpr int WPB = 4;                                  // warps per CTA
     static int per_sm = 0;
     static int sms = 0;
     if (per_sm == 0) {
         int dev = 0;
         LGD_CHECK_CUDA(cudaGetDevice(&dev));
         LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gol_bits_kernel<T>, 128, 0));
+        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gol_bits_kernel<T>, 32 * WPB, 0));
         per_sm = std::max(1, per_sm);
     }
     const int nw = g.desc.nx / 32;
     const int xwarps = (nw + 29) / 30;
-    const long long want = 1LL * sms * per_sm * 4;          // one wave of resident warps
+    const long long want = 1LL * sms * per_sm * WPB;        // one wave of resident warps
     int strip = (int)std::max<long long>(4 * T, ((long long)g.desc.ny * xwarps + want - 1) / want);
     if (shape == 1) strip *= 2;
     if (shape == 2) strip = std::max(2 * T, strip / 2);
@@ -356,7 +357,7 @@ static void launch_gol_bits_typed(Grid& g, int shape)
     const long long warps = (long long)xwarps * ((g.desc.ny + strip - 1) / strip);
     const uint8_t *in = (const uint8_t *)g.m[0].buf[g.cur];
     uint8_t *out = (uint8_t *)g.m[0].buf[1 - g.cur];
-    gol_bits_kernel<T><<<(unsigned)((warps + 3) / 4), 128, 0, g.stream>>>(in, out, g.desc.nx, g.desc.ny,
+    gol_bits_kernel<T><<<(unsigned)((warps + WPB - 1) / WPB), 32 * WPB, 0, g.stream>>>(in, out, g.desc.nx, g.desc.ny,
                                                                          (long)g.pitch_bytes[0], strip, xwarps);
 }
 
