@@ -29,6 +29,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <type_traits>
 
@@ -312,6 +313,22 @@ static long long resident_ctas_tb(const void *fn, int threads, int smem)
     return (long long)sms * std::max(1, per_sm);
 }
 
+// resident CTAs of a pass kernel on the device, set up once (the shared
+// memory limit and the query also load the kernel, which CUDA otherwise
+// does at its first launch)
+template<typename CELL, int TB, int WY, int ROWS>
+static long long tb_resident()
+{
+    typedef tbk::Geo<typename CELL::T, TB, WY, ROWS> G;
+    static long long resident = 0;
+    if (resident == 0) {
+        LGD_CHECK_CUDA(cudaFuncSetAttribute(tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
+        resident = resident_ctas_tb((const void *)tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>, G::THREADS, G::SMEM);
+    }
+    return resident;
+}
+
 // Planes per CTA: minimise waves of resident CTAs times input planes per CTA
 // (the chunk plus the 2 TB halo planes); chunks of at least 8 planes.
 static int pick_zchunk_tb(long long xy, int nz, long long resident, int halo)
@@ -348,12 +365,7 @@ static void launch_tb_typed(Grid& g, int dtype)
         g.tbmap_base[src] = base;
         g.tbmap_rows[src] = G::BH;
     }
-    static long long resident = 0;
-    if (resident == 0) {
-        LGD_CHECK_CUDA(cudaFuncSetAttribute(tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
-        resident = resident_ctas_tb((const void *)tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>, G::THREADS, G::SMEM);
-    }
+    const long long resident = tb_resident<CELL, TB, WY, ROWS>();
     const int bx = (g.desc.nx + G::OX - 1) / G::OX;
     const int by = (g.desc.ny + G::OY - 1) / G::OY;
     const int zchunk = pick_zchunk_tb((long long)bx * by, g.desc.nz, resident, 2 * TB);
@@ -398,8 +410,29 @@ int tb_default_depth(const Grid& g)
 //   fixed point  depth 2 (exact two-step sums, one rounding): 16x4, 8x4, 16x2
 //   FP32         depth 2: 8x4, 16x4, 16x2     depth 3: 16x4, 8x4, 16x2
 //                depth 4: 16x4, 8x4, 16x2
+// every pass kernel set up once, on the first pass of any grid
+static void prepare_tb_kernels()
+{
+    static std::once_flag once;
+    std::call_once(once, [] {
+        (void)tb_resident<Jacobi7FixTwoStep, 2, 16, 4>();
+        (void)tb_resident<Jacobi7FixTwoStep, 2, 8, 4>();
+        (void)tb_resident<Jacobi7FixTwoStep, 2, 16, 2>();
+        (void)tb_resident<Jacobi7F32, 2, 8, 4>();
+        (void)tb_resident<Jacobi7F32, 2, 16, 4>();
+        (void)tb_resident<Jacobi7F32, 2, 16, 2>();
+        (void)tb_resident<Jacobi7F32, 3, 16, 4>();
+        (void)tb_resident<Jacobi7F32, 3, 8, 4>();
+        (void)tb_resident<Jacobi7F32, 3, 16, 2>();
+        (void)tb_resident<Jacobi7F32, 4, 16, 4>();
+        (void)tb_resident<Jacobi7F32, 4, 8, 4>();
+        (void)tb_resident<Jacobi7F32, 4, 16, 2>();
+    });
+}
+
 void launch_jacobi7_tb(Grid& g, int depth, int shape)
 {
+    prepare_tb_kernels();
     const int i64 = CU_TENSOR_MAP_DATA_TYPE_INT64;
     const int f32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
