@@ -320,11 +320,20 @@ public:
         this->stepNum = initializer->startStep();
         box = initializer->gridBox();
         simArea << box;
-        hostGrid = new HostGrid(box);
-        initializer->grid(hostGrid);
-        view = new WriterView(&handle, hostGrid, box);
-        createDevice();
-        upload();
+        // a failing Initializer or device leaves nothing behind (the base
+        // class still owns and deletes the Initializer)
+        try {
+            hostGrid = new HostGrid(box);
+            initializer->grid(hostGrid);
+            view = new WriterView(&handle, hostGrid, box);
+            createDevice();
+            upload();
+        } catch (...) {
+            if (handle) lgd_gpu_destroy(handle);
+            delete view;
+            delete hostGrid;
+            throw;
+        }
     }
 
     virtual ~GB300Simulator()

@@ -592,6 +592,65 @@ static void testTestCellConformance()
     runConformance<TestCellSoA3dTorus>(Coord<3>(54, 20, 13), 0, 7, 1, Coord<3>(64, 2, 3));
 }
 
+// Failures made on the host (no device fault): a Writer that throws in the
+// middle of run(), an Initializer that throws while filling the grid, and
+// one whose grid is empty.  The exception reaches the caller, the simulator
+// is destroyed cleanly, and the library keeps working afterwards.
+class ThrowingWriter : public Writer<JacobiCell> {
+public:
+    explicit ThrowingWriter(unsigned at) : Writer<JacobiCell>("throw", 1), at(at) {}
+    Writer<JacobiCell> *clone() const { return new ThrowingWriter(at); }
+    void stepFinished(const GridType&, unsigned step, WriterEvent)
+    {
+        if (step == at) throw std::runtime_error("writer failed on purpose");
+    }
+
+private:
+    unsigned at;
+};
+
+class ThrowingInit : public JacobiInit {
+public:
+    ThrowingInit() : JacobiInit(Coord<3>(8, 8, 8), 4) {}
+    void grid(GridBase<JacobiCell, 3> *) { throw std::runtime_error("initializer failed on purpose"); }
+};
+
+static void testHostFailuresPropagate()
+{
+    bool thrown = false;
+    {
+        GB300Simulator<JacobiCell> sim(new JacobiInit(Coord<3>(16, 12, 10), 10));
+        sim.addWriter(new ThrowingWriter(6));
+        try {
+            sim.run();
+        } catch (const std::runtime_error& e) {
+            thrown = std::string(e.what()) == "writer failed on purpose";
+        }
+        EXPECT(thrown);
+        EXPECT(sim.getStep() == 6);
+    }
+    thrown = false;
+    try {
+        GB300Simulator<JacobiCell> sim(new ThrowingInit());
+    } catch (const std::runtime_error& e) {
+        thrown = std::string(e.what()) == "initializer failed on purpose";
+    }
+    EXPECT(thrown);
+    thrown = false;
+    try {
+        GB300Simulator<JacobiCell> sim(new JacobiInit(Coord<3>(0, 4, 4), 3));
+    } catch (const std::exception&) {
+        thrown = true;
+    }
+    EXPECT(thrown);
+    // the library still works after the failures
+    GB300Simulator<JacobiCell> sim(new JacobiInit(Coord<3>(12, 9, 7), 5));
+    sim.run();
+    const GridBase<JacobiCell, 3> *grid = sim.getGrid();
+    const std::vector<double> expect = cpuJacobi(Coord<3>(12, 9, 7), 5);
+    EXPECT(grid->get(Coord<3>(3, 4, 5)).temp == expect[(5 * 9 + 4) * 12 + 3]);
+}
+
 // ----------------------------------------------------- Game of Life (2D torus)
 class LifeCell {
 public:
@@ -660,6 +719,7 @@ int main()
     testGliderCrossesTorus();
     testTestCellConformance();
     testStatistics();
+    testHostFailuresPropagate();
     if (failures) {
         std::printf("%d failure(s)\n", failures);
         return 1;
