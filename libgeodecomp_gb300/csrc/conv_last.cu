@@ -211,16 +211,15 @@ bool last_conv_applicable(int nx, int ny, int channels)
 void last_conv(const void *h, const float *w, const float *bias, float *out, bool add_to_u, int nx, int ny, int nz,
                int batch, cudaStream_t stream)
 {
-    static bool configured = false;
-    static int sms = 0;
-    if (!configured) {
+    // set up once per process (a static's initialiser runs once, thread-safely)
+    static const int sms = [] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(last::last_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             last::SMEM));
-        int dev = 0;
+        int dev = 0, count = 0;
         LGD_CHECK_CUDA(cudaGetDevice(&dev));
-        LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        configured = true;
-    }
+        LGD_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
+        return count;
+    }();
     // z chunks: about four resident CTAs' worth of tiles per SM (two waves
     // of two), chunks of at least 8 planes (two extra input planes each)
     const long long xy = (long long)(nx / last::TX) * (ny / last::TY) * batch;

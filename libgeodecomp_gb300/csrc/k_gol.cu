@@ -303,12 +303,12 @@ bool gol_tb_applicable(const Grid& g)
 // generation per pass), 1 = twice as tall, 2 = half as tall
 static int sm_count()
 {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, count = 0;
         LGD_CHECK_CUDA(cudaGetDevice(&dev));
-        LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    }
+        LGD_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
+        return count;
+    }();
     return sms;
 }
 
@@ -317,11 +317,11 @@ static int sm_count()
 template<int T>
 static int gol_tb_per_sm()
 {
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gol_tb_kernel<T>, 128, 0));
-        per_sm = std::max(1, per_sm);
-    }
+    static const int per_sm = [] {
+        int n = 0;
+        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gol_tb_kernel<T>, 128, 0));
+        return std::max(1, n);
+    }();
     return per_sm;
 }
 
@@ -354,11 +354,11 @@ constexpr int GOL_BITS_WPB = 4;                             // warps per CTA of 
 template<int T>
 static int gol_bits_per_sm()
 {
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gol_bits_kernel<T>, 32 * GOL_BITS_WPB, 0));
-        per_sm = std::max(1, per_sm);
-    }
+    static const int per_sm = [] {
+        int n = 0;
+        LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gol_bits_kernel<T>, 32 * GOL_BITS_WPB, 0));
+        return std::max(1, n);
+    }();
     return per_sm;
 }
 

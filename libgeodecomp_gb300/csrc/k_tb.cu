@@ -320,12 +320,11 @@ template<typename CELL, int TB, int WY, int ROWS>
 static long long tb_resident()
 {
     typedef tbk::Geo<typename CELL::T, TB, WY, ROWS> G;
-    static long long resident = 0;
-    if (resident == 0) {
+    static const long long resident = [] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
-        resident = resident_ctas_tb((const void *)tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>, G::THREADS, G::SMEM);
-    }
+        return resident_ctas_tb((const void *)tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>, G::THREADS, G::SMEM);
+    }();
     return resident;
 }
 

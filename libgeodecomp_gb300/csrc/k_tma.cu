@@ -496,12 +496,12 @@ static void launch_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.tmap_base[src] = g.m[0].buf[src];
     }
     const int smem = tmak::S * tmak::Box<T>::SLOT;
-    static bool configured = false;
-    if (!configured) {
+    static const bool configured = [smem] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::jacobi7_tma_kernel<CELL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             smem));
-        configured = true;
-    }
+        return true;
+    }();
+    (void)configured;
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
     const long long xy = (long long)bx * by;
@@ -553,11 +553,10 @@ static void launch_varcoef_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.vtmap_base[src][1] = kbuf;
     }
     const int smem = tmak::VC_S * tmak::vc::Lay<R>::SLOT;
-    static long long resident = 0;
-    if (resident == 0) {
+    static const long long resident = [smem] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::varcoef_tma_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        resident = tmak::resident_ctas((const void *)tmak::varcoef_tma_kernel<R>, tmak::THREADS, smem);
-    }
+        return tmak::resident_ctas((const void *)tmak::varcoef_tma_kernel<R>, tmak::THREADS, smem);
+    }();
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
     const int zchunk = tmak::pick_zchunk((long long)bx * by, g.desc.nz, resident);
