@@ -22,21 +22,28 @@ HBM.
   e2e       the same metric through the C ABI with host buffers: upload
             from pinned host memory, the configuration's run length of time
             steps, download of the result - per e2e step.
+  secondary the other configurations, each measured the same way (value,
+            roofline with traffic, e2e where the data fits a host round
+            trip, the oracle on the host cores as cpu_baseline, clocks):
+            Game of Life 8192^2, SELL-C-sigma diffusion on 4,194,304 nodes,
+            the 512-cavity D3Q19 ensemble, variable-coefficient diffusion
+            256^3 and Jacobi-7 512^3 in FP32.  --no-secondary skips them.
 
-Other workloads (--workload): gol_u8_8192 (Game of Life 8192^2 torus),
-sell_f64_4m (SELL-C-sigma diffusion, 4,194,304 nodes, C=32, sigma=256),
+Other workloads as the headline (--workload): gol_u8_8192, sell_f64_4m,
 jacobi7_f64_ieee_512 (the bit-exact IEEE FP64 kernel alone),
-lbm_d3q19_ensemble_512 (512 uneven D3Q19 cavities, one persistent launch per
-step), varcoef_f32_256 (variable-coefficient diffusion, 256^3 FP32 torus);
---surrogate runs the learned-surrogate time-to-solution benchmark.
+jacobi7_f32_512, lbm_d3q19_ensemble_512, varcoef_f32_256; --surrogate runs
+the learned-surrogate time-to-solution benchmark.
 
 --impl reference times the reference's CPU algorithm on this machine's host
-cores: the C restatement in oracle/ (the reference itself is not built on
-this machine), OpenMP over all cores, on whole time steps of the same input.
+cores: the C restatement in oracle/ (the reference's own sources are not on
+this machine), OpenMP over all cores, on whole time steps of the same input,
+with the same config block as the GPU arm.
 
-Under torchrun (--gpus N > 1) every rank advances its own replica (the
-workload is replicated, not sharded: weak scaling, no collective on the data
-path); rank 0 prints the line with the max time over ranks.
+Under torchrun (--gpus N > 1) the structured workloads are decomposed into
+z-slabs, one per rank (weak scaling: every rank owns a 512^3 slab of a
+512 x 512 x 512N grid), with a ghost-zone exchange of R*T planes every T
+steps (libgeodecomp_gb300.slabs); rank 0 prints the line with the max time
+over ranks.  Other workloads run one replica per rank.
 """
 from __future__ import annotations
 
@@ -55,6 +62,18 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 JACOBI_METRIC = "Jacobi3D GLUPS & HBM GB/s vs 8 TB/s"
+METRICS = {"gol_u8_8192": "Game of Life GLUPS", "sell_f64_4m": "SELL-C-sigma diffusion GB/s and s/step",
+           "lbm_d3q19_ensemble_512": "D3Q19 ensemble GLUPS (one persistent launch per step)",
+           "varcoef_f32_256": "variable-coefficient diffusion GLUPS"}
+DTYPES = {"gol_u8_8192": "u8", "lbm_d3q19_ensemble_512": "f32", "varcoef_f32_256": "f32", "jacobi7_f32_512": "f32",
+          "sell_f64_4m": "f64", "jacobi7_f64_ieee_512": "f64",
+          "jacobi7_f64_512": "f64 (values on the device in 64-bit fixed point, integer arithmetic)"}
+WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "jacobi7_f32_512", "gol_u8_8192", "sell_f64_4m",
+                  "lbm_d3q19_ensemble_512", "varcoef_f32_256"]
+# secondary configurations of the default run: (workload, timed steps, warm-up steps, e2e)
+SECONDARY = [("gol_u8_8192", 1000, 32, True), ("sell_f64_4m", 200, 10, True),
+             ("varcoef_f32_256", 1024, 8, True), ("jacobi7_f32_512", 102, 6, True),
+             ("lbm_d3q19_ensemble_512", 10, 2, False)]
 
 
 def load_peaks():
@@ -138,6 +157,55 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ------------------------------------------------------ workload configs
+def workload_config(name: str, args, world: int = 1) -> dict:
+    """The configuration block of a workload: what runs, on which input.
+
+    Both arms (the GPU library and the reference's CPU algorithm) print
+    this same block, so their lines describe the same workload."""
+    size = getattr(args, "size", 512)
+    if name.startswith("jacobi7"):
+        f32 = name.startswith("jacobi7_f32")
+        ieee = "ieee" in name
+        cfg = {"workload": name if size == 512 else name.replace("512", str(size)),
+               "grid": [size, size, size], "boundary": "constant 0", "cells": size ** 3,
+               "initial": "U[0,1) seed 42", "cell_update": "(c+n+s+e+w+t+b)*(1/7)",
+               "cell": "FP32" if f32 else "FP64 IEEE" if ieee else "FP64, 64-bit fixed point on the device",
+               "l2": "inputs larger than L2 (%d MiB per buffer)" % (size ** 3 * (4 if f32 else 8) >> 20)}
+        if not ieee:
+            tb = getattr(args, "time_block", 0)
+            cfg["time_block"] = ("library default (%d steps per pass)" % (3 if f32 else 2)) if tb == 0 else tb
+    elif name == "gol_u8_8192":
+        cfg = {"workload": name, "grid": [8192, 8192], "boundary": "torus", "cells": 8192 * 8192,
+               "initial": "Bernoulli(0.3) seed 42", "run_steps": 1000,
+               "generations_per_pass": "library default (16, bit-sliced)",
+               "l2": "both buffers (128 MiB) about L2-sized; no flush between steps"}
+    elif name == "sell_f64_4m":
+        cfg = {"workload": name, "nodes": 4194304, "C": 32, "sigma": 256, "degree": "power law alpha=2 on [4,64]",
+               "weights": "U[0,1) row-normalised to 0.9", "update": "x' = 0.1 x + W x", "run_steps": 200,
+               "l2": "matrix (547 MiB) larger than L2; x (32 MiB) L2-resident"}
+    elif name == "varcoef_f32_256":
+        cfg = {"workload": name, "grid": [256, 256, 256], "boundary": "torus", "cells": 256 ** 3,
+               "kappa": "GRF length 16 mapped to [0.02, 0.15]", "initial": "GRF length 16 on [0, 1]",
+               "run_steps": 4096, "l2": "u, k and u' (192 MiB) larger than L2; no flush between steps"}
+    elif name == "lbm_d3q19_ensemble_512":
+        n = getattr(args, "lbm_instances", 512)
+        cfg = {"workload": name, "instances": n, "edges": "uniform {32..%d}" % getattr(args, "lbm_edge_max", 192),
+               "omega": "uniform [1.0, 1.9)", "lid": 0.05, "precision": "FP32", "run_steps": 500,
+               "l2": "populations far larger than L2"}
+    else:
+        raise ValueError(name)
+    if world > 1:
+        cfg["parallelism"] = ("z-slabs, %d ranks" % world) if slab_capable(name) else ("replicas, %d ranks" % world)
+    else:
+        cfg["parallelism"] = "single GPU"
+    return cfg
+
+
+def slab_capable(name: str) -> bool:
+    return name.startswith("jacobi7") or name == "varcoef_f32_256"
+
+
 # ---------------------------------------------------------------- workloads
 class JacobiWorkload:
     run_steps = 100
@@ -153,18 +221,13 @@ class JacobiWorkload:
         self.metric = JACOBI_METRIC
         self.unit = "GLUPS"
         self.units = int(np.prod(self.shape))
-        self.dtype = "f32" if f32 else "f64" if ieee else \
-            "f64 (values on the device in 64-bit fixed point, integer arithmetic)"
         if f32:
             self.bytes_per_unit = 8
         cell = lgd.CELL_JACOBI7_F32 if f32 else lgd.CELL_JACOBI7_F64 if ieee else lgd.CELL_JACOBI7_F64_FIX
         self.g = lgd.Grid(cell, self.shape, periodic=0)
         self.g.fill_uniform(0, seed=42, stream=workloads.STREAM_GRID)
         self.time_block = 0
-        self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "constant 0",
-                       "cells": self.units,
-                       "l2": "inputs larger than L2 (%d MiB per buffer)" % (self.units * (4 if f32 else 8) >> 20),
-                       "cell_update": "(c+n+s+e+w+t+b)*(1/7)"}
+        self.setup = {}
 
     def stream(self):
         p = self.lgd.ctypes.c_void_p()
@@ -179,12 +242,13 @@ class JacobiWorkload:
         self.g.set_time_block(depth)
         self.g.set_time_block_shape(shape)
         self.time_block = depth
-        self.config["time_block"] = "library default" if depth == 0 else depth
 
     def traffic_key(self):
         """Key of the committed ncu traffic line: the workload, plus _tb<d>
         when d > 1 steps are fused per pass (the library's default depth is
         3 for the FP32 cell, 2 for the fixed-point cell)."""
+        if self.ieee:
+            return self.name
         depth = self.time_block or (3 if self.f32 else 2)
         depth = depth if self.f32 else min(depth, 2)
         return self.name if depth <= 1 else "%s_tb%d" % (self.name, depth)
@@ -222,14 +286,12 @@ class GoLWorkload:
         from libgeodecomp_gb300 import lgd, workloads
         self.lgd = lgd
         self.name = "gol_u8_8192"
-        self.metric = "Game of Life GLUPS"
+        self.metric = METRICS[self.name]
         self.unit = "GLUPS"
         self.units = int(np.prod(self.shape))
-        self.dtype = "u8"
         self.g = lgd.Grid(lgd.CELL_GOL_U8, self.shape, periodic=3)
         self.g.fill_bernoulli(0.3, seed=42, stream=workloads.STREAM_GRID)
-        self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "torus", "cells": self.units,
-                       "l2": "both buffers (128 MiB) about L2-sized; no flush between steps"}
+        self.setup = {}
 
     stream = JacobiWorkload.stream
     step = JacobiWorkload.step
@@ -238,11 +300,13 @@ class GoLWorkload:
     e2e_run = JacobiWorkload.e2e_run
     close = JacobiWorkload.close
 
+    def traffic_key(self):
+        return self.name
+
     def set_time_block(self, depth, shape=0):
         """Generations fused per pass (0 = the library's default, 16)."""
         self.g.set_time_block(depth)
         self.g.set_time_block_shape(shape)
-        self.config["generations_per_pass"] = "library default (16, bit-sliced)" if depth == 0 else depth
 
     def host_buffers(self, torch):
         hin = torch.empty(self.units, dtype=torch.uint8, pin_memory=True).numpy().reshape(self.shape)
@@ -259,7 +323,7 @@ class SellWorkload:
         from libgeodecomp_gb300 import lgd, workloads
         self.lgd = lgd
         self.name = "sell_f64_4m"
-        self.metric = "SELL-C-sigma diffusion GB/s and s/step"
+        self.metric = METRICS[self.name]
         self.unit = "GLUPS"
         rp, col, w = workloads.powerlaw_graph(self.n, seed=42)
         self.nnz = int(col.size)
@@ -280,13 +344,12 @@ class SellWorkload:
         # + x' write) + 4 B row length, 4 B per chunk offset
         self.bytes_per_step = 12 * self.nnz + 20 * self.n + 4 * n_chunks
         self.bytes_per_unit = self.bytes_per_step / self.n
-        self.dtype = "f64"
-        self.config = {"workload": self.name, "nodes": self.n, "nnz": self.nnz,
-                       "slots": int(self.s["values"].size), "C": 32, "sigma": 256,
-                       "degree": "power law alpha=2 on [4,64]",
-                       "l2": "matrix (%d MiB) larger than L2; x (32 MiB) L2-resident" % (12 * self.nnz >> 20),
-                       "build_s": {"host_builder": round(host_build, 3),
-                                   "gpu_builder_from_host_csr": round(gpu_build, 4)}}
+        self.setup = {"nnz": self.nnz, "slots": int(self.s["values"].size),
+                      "build_s": {"host_builder": round(host_build, 3),
+                                  "gpu_builder_from_host_csr": round(gpu_build, 4)}}
+
+    def traffic_key(self):
+        return self.name
 
     def stream(self):
         return self.g.stream()
@@ -329,23 +392,23 @@ class VarcoefWorkload:
         self.lgd = lgd
         self.shape = (edge, edge, edge)
         self.name = "varcoef_f32_%d" % edge
-        self.metric = "variable-coefficient diffusion GLUPS"
+        self.metric = METRICS["varcoef_f32_256"]
         self.unit = "GLUPS"
         self.units = int(np.prod(self.shape))
-        self.dtype = "f32"
         self.u0, kappa = workloads.varcoef_fields(edge, seed=42, length=16.0)
         self.g = lgd.Grid(lgd.CELL_VARCOEF_F32, self.shape, periodic=7)
         self.g.upload(0, self.u0)
         self.g.upload(1, kappa)
-        self.config = {"workload": self.name, "grid": list(self.shape), "boundary": "torus", "cells": self.units,
-                       "kappa": "GRF length 16 mapped to [0.02, 0.15]",
-                       "l2": "u, k and u' (192 MiB) larger than L2; no flush between steps"}
+        self.setup = {}
 
     stream = JacobiWorkload.stream
     step = JacobiWorkload.step
     sync = JacobiWorkload.sync
     launches = JacobiWorkload.launches
     close = JacobiWorkload.close
+
+    def traffic_key(self):
+        return self.name
 
     def host_buffers(self, torch):
         hin = torch.empty(self.units * 4, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
@@ -371,23 +434,24 @@ class LbmWorkload:
         from libgeodecomp_gb300 import lgd, workloads
         self.lgd = lgd
         self.name = "lbm_d3q19_ensemble_512"
-        self.metric = "D3Q19 ensemble GLUPS (one persistent launch per step)"
+        self.metric = METRICS[self.name]
         self.unit = "GLUPS"
-        self.dtype = "f32"
         # the configuration is 512 instances with edges up to 192; smaller
         # ensembles serve profiling captures
         edges, omegas = workloads.lbm_ensemble(instances, seed=42, edge_max=edge_max)
         self.e = lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=4)
         self.units, self.items = self.e.info()
+        t0 = time.perf_counter()
         if tune:
             (ty, th, ct), best = self.e.tune(trial_steps=2)
             self.e.reset()
         else:
             ty, th, ct = self.e.config()
-        self.config = {"workload": self.name, "instances": 512, "edges": "uniform {32..192}",
-                       "omega": "uniform [1.0, 1.9)", "lid": 0.05, "cells": self.units, "work_items": self.items,
-                       "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct},
-                       "l2": "166 GB of populations, far larger than L2"}
+        self.setup = {"cells": self.units, "work_items": self.items, "tune_s": round(time.perf_counter() - t0, 2),
+                      "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct}}
+
+    def traffic_key(self):
+        return self.name
 
     def stream(self):
         return self.e.stream()
@@ -400,12 +464,6 @@ class LbmWorkload:
 
     def launches(self):
         return self.e.launch_count()
-
-    def host_buffers(self, torch):
-        return None, None
-
-    def e2e_run(self, hin, hout):
-        raise NotImplementedError
 
     def looped_ms(self, torch, steps):
         st = torch.cuda.ExternalStream(self.e.stream())
@@ -421,15 +479,15 @@ class LbmWorkload:
         self.e.close()
 
 
-def make_workload(name, size=512, lbm_instances=512, lbm_edge_max=192, lbm_tune=True):
+def make_workload(name, args):
     if name == "lbm_d3q19_ensemble_512":
-        return LbmWorkload(instances=lbm_instances, edge_max=lbm_edge_max, tune=lbm_tune)
+        return LbmWorkload(instances=args.lbm_instances, edge_max=args.lbm_edge_max, tune=not args.lbm_no_tune)
     if name == "jacobi7_f64_512":
-        return JacobiWorkload(ieee=False, edge=size)
+        return JacobiWorkload(ieee=False, edge=args.size)
     if name == "jacobi7_f64_ieee_512":
-        return JacobiWorkload(ieee=True, edge=size)
+        return JacobiWorkload(ieee=True, edge=args.size)
     if name == "jacobi7_f32_512":
-        return JacobiWorkload(ieee=False, edge=size, f32=True)
+        return JacobiWorkload(ieee=False, edge=args.size, f32=True)
     if name == "gol_u8_8192":
         return GoLWorkload()
     if name == "sell_f64_4m":
@@ -439,23 +497,20 @@ def make_workload(name, size=512, lbm_instances=512, lbm_edge_max=192, lbm_tune=
     raise ValueError(name)
 
 
-WORKLOAD_NAMES = ["jacobi7_f64_512", "jacobi7_f64_ieee_512", "jacobi7_f32_512", "gol_u8_8192", "sell_f64_4m", "lbm_d3q19_ensemble_512",
-                  "varcoef_f32_256"]
-METRICS = {"gol_u8_8192": "Game of Life GLUPS", "sell_f64_4m": "SELL-C-sigma diffusion GB/s and s/step",
-           "lbm_d3q19_ensemble_512": "D3Q19 ensemble GLUPS (one persistent launch per step)",
-           "varcoef_f32_256": "variable-coefficient diffusion GLUPS"}
-DTYPES = {"gol_u8_8192": "u8", "lbm_d3q19_ensemble_512": "f32", "varcoef_f32_256": "f32", "jacobi7_f32_512": "f32"}
-
-
 # ------------------------------------------------------------------ helpers
-def dist_setup():
+def dist_setup(backend: str = "gloo"):
+    """torch.distributed from torchrun's environment: NCCL where ranks
+    exchange device data (the slab decomposition), gloo otherwise."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("gloo")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local, dist
 
 
@@ -468,7 +523,8 @@ def max_over_ranks(dist, v: float) -> float:
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -487,68 +543,138 @@ def time_steps(torch, w, steps):
     return start.elapsed_time(end)
 
 
-def run_gpu(args, world, rank, local, dist):
-    import torch
-    torch.cuda.set_device(local)
-    w = make_workload(args.workload, args.size, args.lbm_instances, args.lbm_edge_max, not args.lbm_no_tune)
-    if hasattr(w, "set_time_block"):
-        w.set_time_block(args.time_block, args.time_block_shape)
-    w.step(args.warmup)
+def roofline_of(w, ms, steps, launches, peak, peak_kind):
+    """Per launch: one pass over memory, which advances steps / launches time
+    steps (1 without temporal blocking); algorithmic bytes of a pass are
+    bytes_per_unit per cell (every cell read once and written once)."""
+    launch_ms = ms / max(1, launches)
+    algo_bytes = w.units * w.bytes_per_unit
+    achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4),
+                "peak_source": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured"
+                else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": int(algo_bytes), "launch_ms": round(launch_ms, 4),
+                "steps_per_launch": round(steps / max(1, launches), 3), "traffic": profile_traffic(w.traffic_key())}
+    if launches and launches < steps:
+        # the same time with the algorithmic bytes of every time step (per
+        # lattice update: one read and one write per cell), i.e. the HBM
+        # bandwidth a one-step-per-pass code would need for this GLUPS
+        eff = w.units * w.bytes_per_unit * steps / (ms * 1e-3) / 1e9
+        roofline["effective_gbs_one_step_per_pass"] = round(eff, 1)
+        roofline["frac_one_step_per_pass"] = round(eff / peak, 4)
+    return roofline
+
+
+def e2e_of(w, torch, runs, dist=None, world=1):
+    """The workload's run through the C ABI with host buffers: upload from
+    pinned memory, run_steps time steps, download - averaged over runs."""
+    hin, hout = w.host_buffers(torch)
+    w.e2e_run(hin, hout)     # warm-up
+    runs = max(1, runs)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(runs):
+        bi, bo = w.e2e_run(hin, hout)
+    t1 = time.perf_counter()
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, t1 - t0)
+    return {"value": round(w.units * w.run_steps * runs * world / e2e_s / 1e9, 3), "unit": w.unit,
+            "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
+            "step": "upload from pinned host + %d time steps + download, through the C ABI" % w.run_steps,
+            "ms_per_step": round(e2e_s * 1e3 / runs, 3)}
+
+
+def measure(torch, w, steps, warmup, local, dist, world, peak, peak_kind):
+    """Warm-up, then exactly `steps` time steps timed with CUDA events between
+    barriers and device synchronisations; clocks sampled meanwhile."""
+    w.step(warmup)
     w.sync()
     launches0 = w.launches()
     barrier(dist)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        ms = time_steps(torch, w, args.steps)
+        ms = time_steps(torch, w, steps)
     torch.cuda.synchronize()
     barrier(dist)
     launches = w.launches() - launches0
     ms = max_over_ranks(dist, ms)
-    clocks = clk.summary()
-    ms_per_step = ms / args.steps
-    value = w.units * args.steps * world / (ms * 1e-3) / 1e9
+    return {"ms": ms, "launches": launches, "clocks": clk.summary(),
+            "value": w.units * steps * world / (ms * 1e-3) / 1e9,
+            "roofline": roofline_of(w, ms, steps, launches, peak, peak_kind)}
 
+
+def run_secondary(torch, args, local, peak, peak_kind):
+    """The other configurations, one compact block each."""
+    out = {}
+    for name, steps, warmup, has_e2e in SECONDARY:
+        t0 = time.perf_counter()
+        try:
+            w = make_workload(name, argparse.Namespace(**dict(vars(args), size=512, time_block=0)))
+            m = measure(torch, w, steps, warmup, local, None, 1, peak, peak_kind)
+            block = {"metric": w.metric, "value": round(m["value"], 3), "unit": w.unit, "steps": steps,
+                     "warmup": warmup, "ms_per_step": round(m["ms"] / steps, 5), "gpu_launches": m["launches"],
+                     "dtype": DTYPES[name], "config": workload_config(name, args), "roofline": m["roofline"],
+                     "clocks": m["clocks"], "setup": w.setup}
+            if name == "sell_f64_4m":
+                block["s_per_step"] = round(m["ms"] / steps * 1e-3, 7)
+            if name == "lbm_d3q19_ensemble_512":
+                lms = w.looped_ms(torch, 4)
+                block["looped_single_grid_launches"] = {"ms_per_step": round(lms, 3),
+                                                        "glups": round(w.units / (lms * 1e-3) / 1e9, 2)}
+                block["e2e"] = None
+                block["e2e_note"] = ("no host round trip: the ensemble's populations are 83 GB per buffer, "
+                                     "about 0.8 s per upload and download at the host link's rate")
+            elif has_e2e and not args.no_e2e:
+                block["e2e"] = e2e_of(w, torch, args.secondary_e2e_runs)
+            w.close()
+            del w
+            torch.cuda.synchronize()
+            block["wall_s"] = round(time.perf_counter() - t0, 1)
+            out[name] = block
+        except Exception as e:      # a failing secondary must not hide the headline
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+    return out
+
+
+def dropin_run(edge=512, steps=100):
+    """GB300Simulator::run() of the C++ example program (a LibGeoDecomp-style
+    application on the drop-in): wall time of run() - initializer, upload,
+    the steps, a writer reading every cell - and of the steps alone."""
+    from libgeodecomp_gb300 import build
+    src = os.path.join(ROOT, "libgeodecomp_gb300", "examples", "jacobi3d_dropin.cpp")
+    libdir = os.path.join(ROOT, "libgeodecomp_gb300")
+    exe = os.path.join(tempfile.mkdtemp(), "jacobi3d_dropin")
+    build.build()
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I",
+                    os.path.join(libdir, "include"), src, "-L", libdir, "-llgd_gb300", "-Wl,-rpath," + libdir,
+                    "-o", exe], check=True, capture_output=True, text=True)
+    res = subprocess.run([exe, str(edge), str(steps)], check=True, capture_output=True, text=True, timeout=600)
+    out = json.loads(res.stdout.strip().splitlines()[-1])
+    out["program"] = "libgeodecomp_gb300/examples/jacobi3d_dropin.cpp (%d^3, %d steps)" % (edge, steps)
+    return out
+
+
+def run_gpu(args, world, rank, local, dist):
+    import torch
+    torch.cuda.set_device(local)
     peak, peak_kind = load_peaks()
-    # per launch: one pass over memory, which advances steps_per_launch
-    # time steps (1 without temporal blocking); algorithmic bytes of a pass
-    # are bytes_per_unit per cell (every cell read once and written once)
-    launch_ms = ms / max(1, launches)
-    algo_bytes = w.units * w.bytes_per_unit
-    achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
-    traffic = profile_traffic(w.traffic_key() if hasattr(w, "traffic_key") else w.name)
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6800 GB/s",
-                "algorithmic_bytes_per_launch": int(algo_bytes), "launch_ms": round(launch_ms, 4),
-                "steps_per_launch": round(args.steps / max(1, launches), 3), "traffic": traffic}
-    if launches and launches < args.steps:
-        # the same time with the algorithmic bytes of every time step (per
-        # lattice update: one read and one write per cell), i.e. the HBM
-        # bandwidth a one-step-per-pass code would need for this GLUPS
-        eff = w.units * w.bytes_per_unit * args.steps / (ms * 1e-3) / 1e9
-        roofline["effective_gbs_one_step_per_pass"] = round(eff, 1)
-        roofline["frac_one_step_per_pass"] = round(eff / peak, 4)
+    if world > 1 and slab_capable(args.workload):
+        return run_slabs(args, world, rank, local, dist, peak, peak_kind)
+    w = make_workload(args.workload, args)
+    if hasattr(w, "set_time_block"):
+        w.set_time_block(args.time_block, args.time_block_shape)
+    m = measure(torch, w, args.steps, args.warmup, local, dist, world, peak, peak_kind)
+    ms, launches = m["ms"], m["launches"]
+    ms_per_step = ms / args.steps
 
     e2e = None
     if not args.no_e2e and args.workload != "lbm_d3q19_ensemble_512":
-        hin, hout = w.host_buffers(torch)
-        w.e2e_run(hin, hout)     # warm-up
-        runs = max(1, args.e2e_runs)
-        barrier(dist)
-        t0 = time.perf_counter()
-        for _ in range(runs):
-            bi, bo = w.e2e_run(hin, hout)
-        t1 = time.perf_counter()
-        barrier(dist)
-        e2e_s = max_over_ranks(dist, t1 - t0)
-        e2e = {"value": round(w.units * w.run_steps * runs * world / e2e_s / 1e9, 3), "unit": w.unit,
-               "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
-               "step": "upload from pinned host + %d time steps + download, through the C ABI" % w.run_steps,
-               "ms_per_step": round(e2e_s * 1e3 / runs, 3)}
+        e2e = e2e_of(w, torch, args.e2e_runs, dist, world)
 
     extra = {}
-    if args.workload == "jacobi7_f64_512" and not args.no_ieee:
-        # the same grid at the other blocking depths (steps fused per pass)
+    if args.workload == "jacobi7_f64_512" and not args.no_ieee and world == 1:
+        # the same grid at the other blocking depth (steps fused per pass)
         sweep = {}
         for depth in (1, 2):         # the fixed-point cell fuses at most two steps
             if depth == min(args.time_block or 2, 2):     # the depth the headline ran at
@@ -561,7 +687,7 @@ def run_gpu(args, world, rank, local, dist):
                                  "hbm_frac_per_pass": round(w.units * 16 / (msd * depth * 1e-3) / 1e9 / peak, 4)}
         extra["time_block_sweep"] = sweep
         w.close()
-        wi = make_workload("jacobi7_f64_ieee_512", args.size)
+        wi = make_workload("jacobi7_f64_ieee_512", args)
         for _ in range(3):
             wi.step(1)
         wi.sync()
@@ -582,30 +708,98 @@ def run_gpu(args, world, rank, local, dist):
         w.close()
     if args.workload == "sell_f64_4m":
         extra["s_per_step"] = round(ms_per_step * 1e-3, 7)
+    if w.setup:
+        extra["setup"] = w.setup
+
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary and args.workload == "jacobi7_f64_512":
+        secondary = run_secondary(torch, args, local, peak, peak_kind)
+        try:
+            extra["dropin_run"] = dropin_run(args.size, 100)
+        except Exception as e:      # the headline does not depend on it
+            extra["dropin_run"] = {"error": "%s: %s" % (type(e).__name__, e)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload, budget_s=args.cpu_seconds)
+        if secondary:
+            for name, block in secondary.items():
+                if "error" not in block:
+                    try:
+                        block["cpu_baseline"] = cpu_baseline(name, budget_s=args.secondary_cpu_seconds)
+                    except Exception as e:
+                        block["cpu_baseline"] = {"error": "%s: %s" % (type(e).__name__, e)}
 
     if rank == 0:
         line = {
-            "metric": w.metric, "value": round(value, 3), "unit": w.unit, "n_gpus": world, "steps": args.steps,
+            "metric": w.metric, "value": round(m["value"], 3), "unit": w.unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": w.dtype,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPES.get(args.workload, "f64"),
             "data": "synthetic (seeded SplitMix64, generated on device or by libgeodecomp_gb300.workloads)",
-            "config": dict(w.config, parallelism="replicas" if world > 1 else "single GPU"),
-            "gpu_launches": launches, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "config": workload_config(args.workload, args, world),
+            "gpu_launches": launches, "roofline": m["roofline"], "e2e": e2e, "cpu_baseline": cpu,
+            "clocks": m["clocks"],
         }
         line.update(extra)
+        if secondary is not None:
+            line["secondary"] = secondary
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 
 
+def run_slabs(args, world, rank, local, dist, peak, peak_kind):
+    """Weak scaling over z-slabs: every rank owns a size^3 slab of the
+    size x size x (size * world) grid and exchanges ghost planes with its
+    neighbours every pass (libgeodecomp_gb300.slabs)."""
+    import torch
+    from libgeodecomp_gb300 import lgd, slabs
+    cell = {"jacobi7_f64_512": lgd.CELL_JACOBI7_F64_FIX, "jacobi7_f64_ieee_512": lgd.CELL_JACOBI7_F64,
+            "jacobi7_f32_512": lgd.CELL_JACOBI7_F32, "varcoef_f32_256": lgd.CELL_VARCOEF_F32}[args.workload]
+    n = 256 if args.workload == "varcoef_f32_256" else args.size
+    comm = slabs.TorchComm(dist, device=True)
+    s = slabs.SlabGrid(cell, (n * world, n, n), comm, periodic=7 if args.workload == "varcoef_f32_256" else 0,
+                       ghost=args.slab_ghost, time_block=args.time_block)
+    if args.workload == "varcoef_f32_256":
+        from libgeodecomp_gb300 import workloads
+        u0, kappa = workloads.varcoef_fields(n, seed=42, length=16.0)
+        s.upload(0, np.concatenate([u0] * world).astype(np.float32))
+        s.upload(1, np.concatenate([kappa] * world).astype(np.float32))
+    else:
+        s.fill_uniform(seed=42)
+    s.step(args.warmup)
+    s.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        s.step(args.steps)
+        s.synchronize()
+        dt = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    barrier(dist)
+    dt = max_over_ranks(dist, dt)
+    units = n * n * n
+    value = units * world * args.steps / dt / 1e9
+    launches = s.launch_count()
+    if rank == 0:
+        line = {"metric": JACOBI_METRIC if args.workload.startswith("jacobi7") else METRICS[args.workload],
+                "value": round(value, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": DTYPES.get(args.workload, "f64"),
+                "data": "synthetic (seeded SplitMix64, generated on device)",
+                "config": workload_config(args.workload, args, world), "gpu_launches": launches,
+                "timing": "host clock around the ranks' steps (ghost exchanges included), max over ranks",
+                "slabs": s.describe(), "e2e": None, "cpu_baseline": None, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    s.close()
+    dist.destroy_process_group()
+
+
 # ------------------------------------------------------------ CPU baseline
 def cpu_stepper(name):
-    """(units per step, function advancing the input by s steps) of the
-    oracle for a workload."""
+    """(units per step, state, function advancing the state by s steps) of
+    the oracle for a workload."""
     import oracle
     from libgeodecomp_gb300 import workloads
     if name.startswith("jacobi7"):
@@ -645,9 +839,9 @@ def cpu_baseline(name: str, budget_s: float = 15.0):
     for about budget_s seconds."""
     import oracle
     units, state, fn = cpu_stepper(name)
-    fn(state, 1)
+    state = fn(state, 1)
     t0 = time.perf_counter()
-    fn(state, 1)
+    state = fn(state, 1)
     one = time.perf_counter() - t0
     steps = max(1, int(budget_s / max(one, 1e-6)))
     t0 = time.perf_counter()
@@ -669,15 +863,17 @@ def run_reference(args, world, rank):
     state = fn(state, args.steps)
     dt = time.perf_counter() - t0
     value = units * args.steps / dt / 1e9
-    w_metric = METRICS.get(args.workload, JACOBI_METRIC)
     line = {
-        "metric": w_metric, "value": round(value, 4), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": DTYPES.get(args.workload, "f64"),
-        "data": "synthetic (seeded SplitMix64)", "config": {"workload": args.workload},
+        "metric": METRICS.get(args.workload, JACOBI_METRIC), "value": round(value, 4), "unit": "GLUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPES.get(args.workload, "f64"),
+        "data": "synthetic (seeded SplitMix64, generated on device or by libgeodecomp_gb300.workloads)",
+        "config": workload_config(args.workload, args, world),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": oracle.max_threads(), "kind": "port",
-                         "sample": "%d whole time steps of the %s input" % (args.steps, args.workload)},
+                         "sample": "%d whole time steps of the %s input%s" % (
+                             args.steps, args.workload, " (rank 0 only, one slab's worth of cells)"
+                             if world > 1 else "")},
         "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -772,13 +968,17 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=WORKLOAD_NAMES, default="jacobi7_f64_512")
     ap.add_argument("--e2e-runs", type=int, default=5)
+    ap.add_argument("--secondary-e2e-runs", type=int, default=3)
     ap.add_argument("--size", type=int, default=512, help="cube edge of the Jacobi workloads (small profiling cases)")
     ap.add_argument("--time-block", type=int, default=0, help="Jacobi steps fused per pass (0 = library default)")
     ap.add_argument("--time-block-shape", type=int, default=0, help="box shape of the fused passes (tuning)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--secondary-cpu-seconds", type=float, default=5.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ieee", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
+    ap.add_argument("--slab-ghost", type=int, default=8, help="ghost planes per side (steps between exchanges)")
     ap.add_argument("--lbm-instances", type=int, default=512, help="ensemble size (smaller for profiling captures)")
     ap.add_argument("--lbm-edge-max", type=int, default=192)
     ap.add_argument("--lbm-no-tune", action="store_true", help="keep the default launch shape (profiling captures)")
@@ -802,7 +1002,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
-    world, rank, local, dist = dist_setup()
+    world, rank, local, dist = dist_setup("nccl" if world > 1 and slab_capable(args.workload) else "gloo")
     run_gpu(args, world, rank, local, dist)
 
 

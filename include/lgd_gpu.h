@@ -29,7 +29,7 @@ extern "C" {
 
 /* ------------------------------------------------------------ status codes
  * Reference counterparts: LGD_ERR_INVALID ~ std::invalid_argument /
- * std::logic_error (storage/*.h), LGD_ERR_RANGE ~ std::out_of_range thrown by
+ * std::logic_error (storage/ headers), LGD_ERR_RANGE ~ std::out_of_range thrown by
  * the size-bucket dispatch (lib/libflatarray/include/libflatarray/macros.hpp:
  * 948-1060), LGD_ERR_CUDA ~ std::runtime_error("CUDA error") from
  * CUDAUtil::checkForError (misc/cudautil.h:48-55). */
@@ -60,16 +60,22 @@ int lgd_gpu_device_count(int *count);
  *                          bit-identical to the reference's SerialSimulator)
  *   LGD_CELL_JACOBI7_F64_FIX same cell with FP64 values at the ABI; on the
  *                          device the grid is held in 64-bit fixed point,
- *                          value = k * 2^(e - 56) with 2^e the smallest power
- *                          of two above every value uploaded so far and the
- *                          edge cell.  The neighbour sum is exact and the
- *                          division by 7 rounds to the nearest unit, so each
- *                          step adds at most 2^(e - 57) absolute error; a
- *                          temporally blocked pass of two steps sums both
- *                          exactly and rounds once (round of the exact
- *                          two-step average, within one unit of two single
- *                          steps).  For GPUs whose FP64 pipe, not memory,
- *                          would bound the IEEE kernel.
+ *                          value = k * 2^(e - 57), 2^e the smallest power of
+ *                          two above the grid's largest |value| and the edge
+ *                          cell.  The neighbour sum is exact and is
+ *                          multiplied by the same double fl(1/7) as the
+ *                          cell's, rounding to the nearest unit, so each step
+ *                          adds at most 2^(e - 58) absolute error and nothing
+ *                          drifts against the IEEE cell; a temporally blocked
+ *                          pass of two steps sums both exactly and rounds
+ *                          once (within one unit of two single steps).  e is
+ *                          raised when an upload needs it and lowered (an
+ *                          exact shift) after every upload and every 256
+ *                          steps when the grid's values have shrunk, so a
+ *                          decaying grid keeps 57 significant bits at its
+ *                          maximum; such a check waits for the device.  For
+ *                          GPUs whose FP64 pipe, not memory, would bound the
+ *                          IEEE kernel.
  *   LGD_CELL_JACOBI7_F32   members {float temp}; same stencil in FP32
  *   LGD_CELL_SUM6_F64      members {double valA, double valB}; valB' = the
  *                          six face neighbours' valA summed in the order
@@ -104,6 +110,16 @@ int lgd_gpu_device_count(int *count);
 #define LGD_CELL_VARCOEF_F32 6
 #define LGD_CELL_VARCOEF_F64 7
 #define LGD_CELL_TEST 8
+/* A user's own cell class, one record of record_bytes per cell (array of
+ * structures, the reference CUDASimulator's device grid of CELL objects,
+ * parallelization/cudasimulator.h:314-429).  The library stores, copies and
+ * snapshots the records; the cell's own update() / updateCUDA() runs in a
+ * kernel compiled from the cell's source in the caller's translation unit
+ * (libgeodecomp_gb300/include/libgeodecomp_gb300/gb300cell.cuh) on the
+ * handle's stream.  Created by lgd_gpu_create_records; lgd_gpu_step,
+ * region updates, fills, checksums and BOV output are not defined for it. */
+#define LGD_CELL_RECORD 9
+#define LGD_RECORD_MAX_BYTES 4096
 
 #define LGD_TEST_VON_NEUMANN 1
 #define LGD_TEST_NANO_STEPS(n) ((n) << 8)
@@ -142,6 +158,30 @@ typedef struct lgd_handle lgd_handle;
  * and this library has no such limit. */
 int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out);
 int lgd_gpu_destroy(lgd_handle *h);
+
+/* A grid of a user's cell records (LGD_CELL_RECORD): desc->cell must be
+ * LGD_CELL_RECORD, desc->flags 0 and desc->edge is unused; record_bytes
+ * (1 .. LGD_RECORD_MAX_BYTES) is sizeof(CELL) and edge_record the edge cell
+ * (Topologies::Cube reads it outside the grid).  Rows of records are pitched
+ * to 128 bytes: record (x, y, z) starts at ptr + (z*ny + y) * pitch +
+ * x * record_bytes.  Replaces the device allocation of CUDASimulator's
+ * constructor for cells without a kernel of their own in this library. */
+int lgd_gpu_create_records(const lgd_grid_desc *desc, size_t record_bytes, const void *edge_record,
+                           lgd_handle **out);
+
+/* The edge record of a record grid: set_edge_record replaces it (the host
+ * grid's setEdge, storage/gridbase.h), edge_record_device gives its device
+ * copy for kernels. */
+int lgd_gpu_set_edge_record(lgd_handle *h, const void *edge_record, size_t bytes);
+int lgd_gpu_edge_record_device(lgd_handle *h, const void **device_edge);
+
+/* The grid's descriptor as created (cell kind, dimensions, periodic axes,
+ * flags, edge values), for code that steps a handle it did not create. */
+int lgd_gpu_get_desc(lgd_handle *h, lgd_grid_desc *out);
+
+/* Counts kernel launches made on the handle's stream by code outside the
+ * library (the record kernels of gb300cell.cuh), for lgd_gpu_launch_count. */
+int lgd_gpu_count_launches(lgd_handle *h, uint64_t n);
 
 /* Host <-> device copy of one member of one buffer (which: 0 = current
  * grid, 1 = next grid); bytes must equal nx*ny*nz*sizeof(member).  Replaces
@@ -194,6 +234,27 @@ int lgd_gpu_fill_bernoulli(lgd_handle *h, int member, int which, uint64_t seed, 
 /* Fixed-point exponent e of an LGD_CELL_JACOBI7_F64_FIX grid. */
 int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
 
+/* Sets the exponent of a fixed-point grid to e (>= the edge cell's bound):
+ * both buffers are rescaled, exactly when e falls (a shift left; values
+ * that would not fit return LGD_ERR_RANGE and leave the grid unchanged),
+ * rounded to nearest when it rises.  pin != 0 keeps e from now on: the
+ * checks after uploads and every 256 steps no longer lower it (an upload
+ * whose values need more still raises it).  For grids that exchange raw
+ * planes (a z-slab decomposition, lgd_gpu_copy_planes), which need one
+ * exponent on every rank. */
+int lgd_gpu_set_fixed_point_exponent(lgd_handle *h, int e, int pin);
+
+/* Raw planes of the slowest axis (z for 3D grids, y for 2D, the whole row
+ * for 1D) in the device representation, row padding included: planes
+ * p0 .. p0 + np - 1 of one member of one buffer to or from buf, which may be
+ * host or device memory (bytes = np * plane_bytes, plane_bytes from
+ * lgd_gpu_plane_bytes).  The ghost-zone exchange of a slab decomposition
+ * (the reference's patch links of HiParSimulator,
+ * parallelization/hiparsimulator.h:60-72, communication/patchlink.h).
+ * Synchronises the handle's stream. */
+int lgd_gpu_plane_bytes(lgd_handle *h, int member, size_t *bytes);
+int lgd_gpu_copy_planes(lgd_handle *h, int member, int which, int p0, int np, void *buf, size_t bytes, int to_grid);
+
 /* Kernel variant for the Jacobi cells (results are identical): 0 (default)
  * TMA-staged shared-memory planes on cube grids with a zero edge cell,
  * otherwise variant 5; 1 shared-memory plane tiles loaded by the threads;
@@ -214,8 +275,10 @@ int lgd_gpu_stream(lgd_handle *h, void **stream);
 /* ------------------------------------------------- allocation-free sum
  * No counterpart in the reference.  Sum of n FP64 values in device memory,
  * written to *d_result (device memory), asynchronously on stream (a
- * cudaStream_t, NULL = the default stream) - the same reduction as
- * lgd_gpu_checksum, for callers that must not allocate device memory: a
+ * cudaStream_t, NULL = the default stream) - the same sum as
+ * lgd_gpu_checksum, added in a different order (blocks of 65536 values and
+ * a tree on the device), so not bit-identical to it - for callers that must
+ * not allocate device memory: a
  * plugin or solver running inside another framework's stream and memory
  * pool, where cudaMalloc/cudaFree would synchronise the device and
  * fragment the pool, or code with a fixed memory budget.  It calls no
@@ -224,7 +287,8 @@ int lgd_gpu_stream(lgd_handle *h, void **stream);
  * Hence n <= LGD_SUM_STATIC_MAX_N (larger n returns LGD_ERR_RANGE), and
  * calls that overlap on the GPU (unordered streams) race on that array.
  * The first call on a device looks the array's address up (no
- * allocation); make that first call before any stream capture. */
+ * allocation); make that first call before any stream capture.  The lookup
+ * is repeated when the device's context changes (after a cudaDeviceReset). */
 #define LGD_SUM_STATIC_CHUNK 65536
 #define LGD_SUM_STATIC_MAX_PARTIALS 16384
 #define LGD_SUM_STATIC_MAX_N (1LL << 30)
@@ -261,6 +325,18 @@ int lgd_snapshot_info(const char *path, int dim, int *dims, unsigned *step, unsi
 int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum);
 
 int lgd_gpu_synchronize(lgd_handle *h);
+
+/* For tests of the timeout path; no counterpart in the reference.  Every
+ * wait of the library's kernels on a copy or a peer is bounded (about two
+ * seconds of clock cycles); a CTA whose wait runs out sets the handle's
+ * error word, waits (bounded) for its own copies in flight and returns, and
+ * the next synchronising call returns LGD_ERR_TIMEOUT.  This call bounds the
+ * single-step TMA Jacobi kernel's waits at wait_cycles (0 = the default)
+ * and, with skip_plane >= 0, makes its first CTA leave that plane's copy
+ * unissued, so that one wait runs out on purpose (nothing faults or hangs:
+ * the wait returns after wait_cycles).  skip_plane = -1 restores normal
+ * steps; a step with a skipped plane leaves incomplete results. */
+int lgd_gpu_test_bounded_waits(lgd_handle *h, long long wait_cycles, int skip_plane);
 
 /* Device pointer and row pitch (bytes) of one member of one buffer; the
  * grid is pitched: row (y, z) starts at ptr + ((z*ny + y) * pitch). */

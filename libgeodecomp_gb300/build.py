@@ -26,7 +26,7 @@ def nvcc() -> str:
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
     deps = [src] + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
-        [os.path.join(os.path.dirname(HERE), "include", "lgd_gpu.h")]
+        glob.glob(os.path.join(os.path.dirname(HERE), "include", "*.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",

@@ -46,6 +46,7 @@ static CellInfo cell_info(int cell)
     case LGD_CELL_VARCOEF_F32:     return {2, {4, 4}, {4, 4}, {false, true}, 3, 3};
     case LGD_CELL_VARCOEF_F64:     return {2, {8, 8}, {8, 8}, {false, true}, 3, 3};
     case LGD_CELL_TEST:            return {1, {64, 0}, {64, 0}, {false, false}, 1, 3};
+    case LGD_CELL_RECORD:          return {1, {0, 0}, {0, 0}, {false, false}, 1, 3};   // size per grid
     default:
         throw Error(LGD_ERR_INVALID, "unknown cell kind " + std::to_string(cell));
     }
@@ -98,16 +99,19 @@ __global__ void from_fix_pitched_kernel(const long long *src, double *dst, int n
 // per-block max |v| (NaN propagates as NaN through fmax's operand order
 // being irrelevant: a NaN block result is turned into +inf so the host sees
 // a non-finite maximum)
-__global__ void absmax_kernel(const double *v, long long n, double *partial)
+__global__ void absmax_kernel(const double *v, long long n, double *partial, unsigned long long *negative)
 {
     __shared__ double red[256];
     double m = 0.0;
     bool bad = false;
+    bool neg = false;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double a = fabs(v[i]);
         bad |= !(a <= 1.7976931348623157e308);
+        neg |= v[i] < 0.0;
         m = fmax(m, a);
     }
+    if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) atomicOr(negative, 1ull);
     red[threadIdx.x] = bad ? __longlong_as_double(0x7ff0000000000000ll) : m;
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1) {
@@ -148,6 +152,68 @@ static void raise_fix_exp(Grid& g, int e)
     g.fix_exp = e;
 }
 
+// max |k| over the cells of one fixed-point buffer (rows of nx cells, pitch
+// elements apart) into *out with atomicMax
+__global__ void fix_absmax_kernel(const long long *buf, int nx, long long rows, long long pitch,
+                                  unsigned long long *out)
+{
+    unsigned long long m = 0;
+    const long long n = (long long)nx * rows;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / nx;
+        const long long v = buf[r * pitch + (i - r * nx)];
+        m = max(m, (unsigned long long)(v < 0 ? -v : v));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+__global__ void shift_fix_kernel(long long *buf, long long n, int shift)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        buf[i] = (long long)((unsigned long long)buf[i] << shift);
+    }
+}
+
+// Lowers fix_exp as far as both buffers and the edge cell allow (the
+// largest |k| just below 2^57 afterwards), shifting both buffers left: no
+// rounding, only unused high bits are traded for fraction bits.  With a
+// zero edge cell a decaying grid keeps 57 significant bits at its maximum
+// instead of losing one per halving.  Synchronises the grid's stream.
+static void lower_fix_exp(Grid& g)
+{
+    if (g.fix_pinned) {
+        g.fix_steps_unchecked = 0;
+        return;
+    }
+    const long long rows = (long long)g.desc.ny * g.desc.nz;
+    const long long pitch = (long long)(g.pitch_bytes[0] / 8);
+    LGD_CHECK_CUDA(cudaMemsetAsync(g.d_fixmax, 0, sizeof(unsigned long long), g.stream));
+    for (int b = 0; b < 2; ++b) {
+        fix_absmax_kernel<<<152 * 4, 256, 0, g.stream>>>((const long long *)g.m[0].buf[b], g.desc.nx, rows, pitch,
+                                                         g.d_fixmax);
+        check_launch("fixed-point maximum");
+        ++g.launches;
+    }
+    unsigned long long m = 0;
+    LGD_CHECK_CUDA(cudaMemcpyAsync(&m, g.d_fixmax, sizeof(m), cudaMemcpyDeviceToHost, g.stream));
+    LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    g.fix_steps_unchecked = 0;
+    if (m == 0) return;                                         // an all-zero grid keeps its exponent
+    int shift = __builtin_clzll(m) - (64 - LGD_FIX_BITS);      // m << shift < 2^57 <= m << (shift + 1)
+    if (g.desc.edge[0] != 0.0) shift = std::min(shift, g.fix_exp - exp_bound(std::fabs(g.desc.edge[0])));
+    shift = std::min(shift, g.fix_exp + 960);                  // stays far inside the double range
+    if (shift <= 0) return;
+    const long long n = (long long)buffer_elems(g, 0);
+    for (int b = 0; b < 2; ++b) {
+        shift_fix_kernel<<<152 * 4, 256, 0, g.stream>>>((long long *)g.m[0].buf[b], n, shift);
+        check_launch("fixed-point rescale");
+        ++g.launches;
+    }
+    g.fix_exp -= shift;
+    LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+}
+
 // --------------------------------------------------------------- helpers
 // Reads (and clears) the device error word that kernels with bounded waits
 // set when a wait gave up; call after the stream is synchronised.
@@ -182,6 +248,8 @@ static double *staging(Grid& g, size_t bytes)
 // Row chunks of a fixed-point transfer: the copy of chunk k overlaps the
 // conversion of its neighbour (16 chunks: 64 MiB each at 512^3 FP64).
 constexpr int XFER_CHUNKS = 16;
+// steps of a fixed-point grid between two checks of its exponent
+constexpr int FIX_CHECK_STEPS = 256;
 constexpr int ABSMAX_BLOCKS = 152;
 
 static void xfer_init(Grid& g)
@@ -292,12 +360,20 @@ int lgd_gpu_device_count(int *count)
     });
 }
 
-int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
+// Allocates a grid; record grids (LGD_CELL_RECORD) take their element size
+// and edge record from the arguments.
+static void create_grid(const lgd_grid_desc *desc, size_t record_bytes, const void *edge_record, lgd_handle **out)
 {
-    return guard([&] {
+    {
         LGD_REQUIRE(desc != nullptr && out != nullptr, LGD_ERR_INVALID, "null argument");
         *out = nullptr;
-        const CellInfo ci = cell_info(desc->cell);
+        CellInfo ci = cell_info(desc->cell);
+        if (desc->cell == LGD_CELL_RECORD) {
+            LGD_REQUIRE(record_bytes >= 1 && record_bytes <= LGD_RECORD_MAX_BYTES, LGD_ERR_INVALID,
+                        "record size out of range (1 .. LGD_RECORD_MAX_BYTES)");
+            LGD_REQUIRE(edge_record != nullptr, LGD_ERR_INVALID, "null edge record");
+            ci.elem[0] = ci.host_elem[0] = (int)record_bytes;
+        }
         LGD_REQUIRE(desc->dim >= ci.dim_min && desc->dim <= ci.dim_max, LGD_ERR_INVALID, "dimension does not match the cell");
         LGD_REQUIRE(desc->nx > 0 && desc->ny > 0 && desc->nz > 0, LGD_ERR_INVALID, "grid dimensions must be positive");
         LGD_REQUIRE(desc->dim == 3 || desc->nz == 1, LGD_ERR_INVALID, "2D grids have nz = 1");
@@ -332,8 +408,19 @@ int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
             }
             g.pitch_elems = g.pitch_bytes[0] / ci.elem[0];
             g.plane_elems = g.pitch_elems * desc->ny;
+            if (desc->cell == LGD_CELL_RECORD) {
+                g.edge_record = (unsigned char *)std::malloc(record_bytes);
+                LGD_REQUIRE(g.edge_record != nullptr, LGD_ERR_NOMEM, "host allocation failed");
+                std::memcpy(g.edge_record, edge_record, record_bytes);
+                LGD_CHECK_CUDA(cudaMalloc(&g.d_edge_record, record_bytes));
+                LGD_CHECK_CUDA(cudaMemcpyAsync(g.d_edge_record, edge_record, record_bytes, cudaMemcpyHostToDevice,
+                                               g.stream));
+            }
             if (desc->cell == LGD_CELL_JACOBI7_F64_FIX) {
                 g.fix_exp = exp_bound(std::fabs(desc->edge[0]));
+                g.fix_nonneg = desc->edge[0] >= 0.0;
+                LGD_CHECK_CUDA(cudaMalloc(&g.d_fixmax, 2 * sizeof(unsigned long long)));
+                LGD_CHECK_CUDA(cudaMemsetAsync(g.d_fixmax, 0, 2 * sizeof(unsigned long long), g.stream));
             }
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
         } catch (...) {
@@ -342,12 +429,142 @@ int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
                     if (g.m[m].buf[b]) cudaFree(g.m[m].buf[b]);
                 }
             }
+            if (g.d_err) cudaFree(g.d_err);
+            if (g.d_fixmax) cudaFree(g.d_fixmax);
+            if (g.d_edge_record) cudaFree(g.d_edge_record);
+            std::free(g.edge_record);
             if (g.stream) cudaStreamDestroy(g.stream);
             delete h;
             throw;
         }
         *out = h;
+    }
+}
+
+int lgd_gpu_create(const lgd_grid_desc *desc, lgd_handle **out)
+{
+    return guard([&] {
+        LGD_REQUIRE(desc == nullptr || desc->cell != LGD_CELL_RECORD, LGD_ERR_INVALID,
+                    "record grids are created by lgd_gpu_create_records");
+        create_grid(desc, 0, nullptr, out);
     });
+}
+
+int lgd_gpu_create_records(const lgd_grid_desc *desc, size_t record_bytes, const void *edge_record,
+                           lgd_handle **out)
+{
+    return guard([&] {
+        LGD_REQUIRE(desc == nullptr || desc->cell == LGD_CELL_RECORD, LGD_ERR_INVALID,
+                    "desc->cell must be LGD_CELL_RECORD");
+        create_grid(desc, record_bytes, edge_record, out);
+    });
+}
+
+int lgd_gpu_set_edge_record(lgd_handle *h, const void *edge_record, size_t bytes)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(g.desc.cell == LGD_CELL_RECORD, LGD_ERR_INVALID, "not a record grid");
+        LGD_REQUIRE(edge_record != nullptr && bytes == (size_t)g.m[0].elem, LGD_ERR_INVALID,
+                    "edge record size does not match the grid's records");
+        std::memcpy(g.edge_record, edge_record, bytes);
+        LGD_CHECK_CUDA(cudaMemcpyAsync(g.d_edge_record, g.edge_record, bytes, cudaMemcpyHostToDevice, g.stream));
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_edge_record_device(lgd_handle *h, const void **device_edge)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(g.desc.cell == LGD_CELL_RECORD, LGD_ERR_INVALID, "not a record grid");
+        LGD_REQUIRE(device_edge != nullptr, LGD_ERR_INVALID, "null output");
+        *device_edge = g.d_edge_record;
+    });
+}
+
+int lgd_gpu_set_fixed_point_exponent(lgd_handle *h, int e, int pin)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(g.desc.cell == LGD_CELL_JACOBI7_F64_FIX, LGD_ERR_INVALID, "not a fixed-point grid");
+        LGD_REQUIRE(e >= exp_bound(std::fabs(g.desc.edge[0])) && e <= 1000 && e >= -960, LGD_ERR_RANGE,
+                    "exponent out of range for the grid's edge cell");
+        if (e > g.fix_exp) {
+            raise_fix_exp(g, e);
+        } else if (e < g.fix_exp) {
+            const long long rows = (long long)g.desc.ny * g.desc.nz;
+            const long long pitch = (long long)(g.pitch_bytes[0] / 8);
+            LGD_CHECK_CUDA(cudaMemsetAsync(g.d_fixmax, 0, sizeof(unsigned long long), g.stream));
+            for (int b = 0; b < 2; ++b) {
+                fix_absmax_kernel<<<152 * 4, 256, 0, g.stream>>>((const long long *)g.m[0].buf[b], g.desc.nx, rows,
+                                                                 pitch, g.d_fixmax);
+                check_launch("fixed-point maximum");
+                ++g.launches;
+            }
+            unsigned long long m = 0;
+            LGD_CHECK_CUDA(cudaMemcpyAsync(&m, g.d_fixmax, sizeof(m), cudaMemcpyDeviceToHost, g.stream));
+            LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            const int shift = g.fix_exp - e;
+            LGD_REQUIRE(m == 0 || (shift < 64 && (m >> (LGD_FIX_BITS - shift)) == 0), LGD_ERR_RANGE,
+                        "the grid's values do not fit the lower exponent");
+            const long long n = (long long)buffer_elems(g, 0);
+            for (int b = 0; b < 2; ++b) {
+                shift_fix_kernel<<<152 * 4, 256, 0, g.stream>>>((long long *)g.m[0].buf[b], n, shift);
+                check_launch("fixed-point rescale");
+                ++g.launches;
+            }
+            g.fix_exp = e;
+        }
+        g.fix_pinned = pin != 0;
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_plane_bytes(lgd_handle *h, int member, size_t *bytes)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, 0);
+        LGD_REQUIRE(bytes != nullptr, LGD_ERR_INVALID, "null output");
+        *bytes = g.pitch_bytes[member] * (g.desc.dim == 3 ? (size_t)g.desc.ny : 1);
+    });
+}
+
+int lgd_gpu_copy_planes(lgd_handle *h, int member, int which, int p0, int np, void *buf, size_t bytes, int to_grid)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        check_member(g, member, which);
+        const int planes = g.desc.dim == 3 ? g.desc.nz : g.desc.ny;
+        LGD_REQUIRE(p0 >= 0 && np >= 0 && p0 + np <= planes, LGD_ERR_RANGE, "planes outside the grid");
+        const size_t plane = g.pitch_bytes[member] * (g.desc.dim == 3 ? (size_t)g.desc.ny : 1);
+        LGD_REQUIRE(bytes == plane * (size_t)np, LGD_ERR_INVALID, "byte count does not match the planes");
+        LGD_REQUIRE(buf != nullptr || np == 0, LGD_ERR_INVALID, "null buffer");
+        char *base = (char *)member_buf(g, member, which) + plane * (size_t)p0;
+        if (np > 0) {
+            if (to_grid) {
+                LGD_CHECK_CUDA(cudaMemcpyAsync(base, buf, bytes, cudaMemcpyDefault, g.stream));
+            } else {
+                LGD_CHECK_CUDA(cudaMemcpyAsync(buf, base, bytes, cudaMemcpyDefault, g.stream));
+            }
+        }
+        LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int lgd_gpu_get_desc(lgd_handle *h, lgd_grid_desc *out)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(out != nullptr, LGD_ERR_INVALID, "null output");
+        *out = g.desc;
+    });
+}
+
+int lgd_gpu_count_launches(lgd_handle *h, uint64_t n)
+{
+    return guard([&] { grid_of(h).launches += n; });
 }
 
 int lgd_gpu_destroy(lgd_handle *h)
@@ -365,6 +582,9 @@ int lgd_gpu_destroy(lgd_handle *h)
         if (g.d_streak_prefix) cudaFree(g.d_streak_prefix);
         if (g.d_partials) cudaFree(g.d_partials);
         if (g.d_err) cudaFree(g.d_err);
+        if (g.d_fixmax) cudaFree(g.d_fixmax);
+        if (g.d_edge_record) cudaFree(g.d_edge_record);
+        std::free(g.edge_record);
         if (g.d_stage) cudaFree(g.d_stage);
         if (g.xfer_ready) {
             cudaStreamSynchronize(g.xfer_stream);
@@ -401,6 +621,7 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
             const int e0 = g.fix_exp;
             xfer_init(g);
             // the copies wait for earlier work of the grid (the staging buffer)
+            LGD_CHECK_CUDA(cudaMemsetAsync(g.d_fixmax + 1, 0, sizeof(unsigned long long), g.stream));
             LGD_CHECK_CUDA(cudaEventRecord(g.xfer_ev[XFER_CHUNKS], g.stream));
             LGD_CHECK_CUDA(cudaStreamWaitEvent(g.xfer_stream, g.xfer_ev[XFER_CHUNKS], 0));
             for (int k = 0; k < K; ++k) {
@@ -410,7 +631,7 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
                 LGD_CHECK_CUDA(cudaEventRecord(g.xfer_ev[k], g.xfer_stream));
                 LGD_CHECK_CUDA(cudaStreamWaitEvent(g.stream, g.xfer_ev[k], 0));
                 absmax_kernel<<<ABSMAX_BLOCKS, 256, 0, g.stream>>>(tmp + r0 * nx, (long long)((r1 - r0) * nx),
-                                                                   partial + (size_t)k * ABSMAX_BLOCKS);
+                                                                   partial + (size_t)k * ABSMAX_BLOCKS, g.d_fixmax + 1);
                 check_launch("max |value|");
                 to_fix_pitched_kernel<<<152 * 2, 256, 0, g.stream>>>(tmp + r0 * nx, dst + r0 * pitch, g.desc.nx,
                                                                     (long long)(r1 - r0), (long long)pitch, e0);
@@ -418,14 +639,32 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
                 g.launches += 2;
             }
             std::vector<double> hpart((size_t)K * ABSMAX_BLOCKS);
+            unsigned long long negative = 0;
             LGD_CHECK_CUDA(cudaMemcpyAsync(hpart.data(), partial, sizeof(double) * hpart.size(), cudaMemcpyDeviceToHost,
                                            g.stream));
+            LGD_CHECK_CUDA(cudaMemcpyAsync(&negative, g.d_fixmax + 1, sizeof(negative), cudaMemcpyDeviceToHost,
+                                           g.stream));
             LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            // sticky: once a grid has held a negative value its steps keep
+            // the sign handling (the results do not depend on it)
+            if (negative) g.fix_nonneg = false;
             double m = std::fabs(g.desc.edge[0]);
             for (double v : hpart) m = std::fmax(m, v);
             LGD_REQUIRE(std::isfinite(m), LGD_ERR_INVALID, "grid holds a non-finite value");
             if (exp_bound(m) > g.fix_exp) {
                 raise_fix_exp(g, exp_bound(m));
+                to_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(tmp, dst, g.desc.nx, (long long)rows,
+                                                                    (long long)pitch, g.fix_exp);
+                check_launch("to fixed point");
+                ++g.launches;
+                LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
+            }
+            // values well below the exponent's range: lower it (both
+            // buffers), then convert the doubles again at the new scale so
+            // that no fraction bit is lost at the boundary
+            const int e_before = g.fix_exp;
+            lower_fix_exp(g);
+            if (g.fix_exp < e_before) {
                 to_fix_pitched_kernel<<<152 * 8, 256, 0, g.stream>>>(tmp, dst, g.desc.nx, (long long)rows,
                                                                     (long long)pitch, g.fix_exp);
                 check_launch("to fixed point");
@@ -495,7 +734,8 @@ int lgd_gpu_write_bov(lgd_handle *h, int member, const char *prefix, unsigned st
         LGD_REQUIRE(prefix != nullptr && variable != nullptr, LGD_ERR_INVALID, "null file prefix or variable name");
         const size_t n = cells_of(g);
         const int elem = g.m[member].elem;
-        LGD_REQUIRE(elem == 1 || elem == 4 || elem == 8, LGD_ERR_UNSUPPORTED, "BOV holds scalar members only");
+        LGD_REQUIRE(g.desc.cell != LGD_CELL_RECORD && (elem == 1 || elem == 4 || elem == 8), LGD_ERR_UNSUPPORTED,
+                    "BOV holds scalar members only");
         std::vector<unsigned char> data(n * elem);
         const int rc = lgd_gpu_download(h, member, 0, data.data(), data.size());
         LGD_REQUIRE(rc == LGD_OK, rc, "download for the BOV snapshot failed");
@@ -543,7 +783,9 @@ static void member_edge_bytes(const Grid& g, int m, unsigned char *out)
 {
     const double e = g.desc.edge[m];
     const int elem = g.m[m].elem;
-    if (g.desc.cell == LGD_CELL_TEST) {
+    if (g.desc.cell == LGD_CELL_RECORD) {
+        std::memcpy(out, g.edge_record, (size_t)elem);
+    } else if (g.desc.cell == LGD_CELL_TEST) {
         // the reference TestInitializer's edge cell: position -1 on every
         // axis, the grid's dimensions, cycle 0, test value 666
         TestRec r;
@@ -738,12 +980,25 @@ int lgd_gpu_step(lgd_handle *h, unsigned nano_step, int count)
     return guard([&] {
         Grid& g = grid_of(h);
         LGD_REQUIRE(count >= 0, LGD_ERR_INVALID, "negative step count");
+        LGD_REQUIRE(g.desc.cell != LGD_CELL_RECORD, LGD_ERR_UNSUPPORTED,
+                    "record grids run the cell's own update() through gb300cell.cuh");
         if (count == 0) return;
         switch (g.desc.cell) {
         case LGD_CELL_JACOBI7_F64:
-        case LGD_CELL_JACOBI7_F64_FIX:
         case LGD_CELL_JACOBI7_F32:
             launch_jacobi7(g, count);
+            break;
+        case LGD_CELL_JACOBI7_F64_FIX:
+            // the exponent follows a decaying grid down: checked after every
+            // FIX_CHECK_STEPS steps (one read of both buffers and a wait),
+            // also inside a long call
+            while (count > 0) {
+                const int k = std::min(count, std::max(1, FIX_CHECK_STEPS - g.fix_steps_unchecked));
+                launch_jacobi7(g, k);
+                g.fix_steps_unchecked += k;
+                count -= k;
+                if (g.fix_steps_unchecked >= FIX_CHECK_STEPS) lower_fix_exp(g);
+            }
             break;
         case LGD_CELL_GOL_U8:
             launch_gol(g, count);
@@ -779,6 +1034,8 @@ int lgd_gpu_update_region(lgd_handle *h, const int *streaks, int n_streaks, unsi
 {
     return guard([&] {
         Grid& g = grid_of(h);
+        LGD_REQUIRE(g.desc.cell != LGD_CELL_RECORD, LGD_ERR_UNSUPPORTED,
+                    "record grids run the cell's own update() through gb300cell.cuh");
         const long long cells = stage_streaks(g, streaks, n_streaks);
         launch_region(g, g.d_streaks, g.d_streak_prefix, n_streaks, cells, nano_step);
     });
@@ -797,10 +1054,14 @@ int lgd_gpu_fill_uniform(lgd_handle *h, int member, int which, uint64_t seed, in
     return guard([&] {
         Grid& g = grid_of(h);
         check_member(g, member, which);
-        LGD_REQUIRE(g.m[member].elem != 1, LGD_ERR_INVALID, "uniform fill needs a floating-point member");
+        LGD_REQUIRE(g.desc.cell != LGD_CELL_RECORD && g.m[member].elem != 1, LGD_ERR_INVALID,
+                    "uniform fill needs a floating-point member");
         if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
             raise_fix_exp(g, 0);   // uniform values lie in [0, 1)
             launch_fill(g, member, which, seed, stream, 2, 0.0, g.fix_exp);
+            const int e_before = g.fix_exp;
+            lower_fix_exp(g);
+            if (g.fix_exp < e_before) launch_fill(g, member, which, seed, stream, 2, 0.0, g.fix_exp);
         } else {
             launch_fill(g, member, which, seed, stream, 0, 0.0, 0);
         }
@@ -813,7 +1074,8 @@ int lgd_gpu_fill_bernoulli(lgd_handle *h, int member, int which, uint64_t seed, 
     return guard([&] {
         Grid& g = grid_of(h);
         check_member(g, member, which);
-        LGD_REQUIRE(g.m[member].elem == 1, LGD_ERR_INVALID, "Bernoulli fill needs a uint8 member");
+        LGD_REQUIRE(g.desc.cell != LGD_CELL_RECORD && g.m[member].elem == 1, LGD_ERR_INVALID,
+                    "Bernoulli fill needs a uint8 member");
         launch_fill(g, member, which, seed, stream, 1, p, 0);
         LGD_CHECK_CUDA(cudaStreamSynchronize(g.stream));
     });
@@ -825,6 +1087,7 @@ int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum)
         Grid& g = grid_of(h);
         check_member(g, member, which);
         LGD_REQUIRE(sum != nullptr, LGD_ERR_INVALID, "null output");
+        LGD_REQUIRE(g.desc.cell != LGD_CELL_RECORD, LGD_ERR_UNSUPPORTED, "records have no numeric sum");
         // the checksum kernel reads through the current/next view
         const int saved = g.cur;
         if (which == 1 && !g.m[member].is_static) g.cur = 1 - g.cur;
@@ -835,6 +1098,16 @@ int lgd_gpu_checksum(lgd_handle *h, int member, int which, double *sum)
             throw;
         }
         g.cur = saved;
+    });
+}
+
+int lgd_gpu_test_bounded_waits(lgd_handle *h, long long wait_cycles, int skip_plane)
+{
+    return guard([&] {
+        Grid& g = grid_of(h);
+        LGD_REQUIRE(wait_cycles >= 0 && skip_plane >= -1, LGD_ERR_INVALID, "negative wait bound or plane");
+        g.test_wait_cycles = wait_cycles;
+        g.test_skip_plane = skip_plane + 1;
     });
 }
 

@@ -211,15 +211,16 @@ bool last_conv_applicable(int nx, int ny, int channels)
 void last_conv(const void *h, const float *w, const float *bias, float *out, bool add_to_u, int nx, int ny, int nz,
                int batch, cudaStream_t stream)
 {
-    // set up once per process (a static's initialiser runs once, thread-safely)
-    static const int sms = [] {
+    // set up once per device
+    static PerDevice<int> setup;
+    const int sms = setup.get([] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(last::last_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             last::SMEM));
         int dev = 0, count = 0;
         LGD_CHECK_CUDA(cudaGetDevice(&dev));
         LGD_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
         return count;
-    }();
+    });
     // z chunks: about four resident CTAs' worth of tiles per SM (two waves
     // of two), chunks of at least 8 planes (two extra input planes each)
     const long long xy = (long long)(nx / last::TX) * (ny / last::TY) * batch;

@@ -458,13 +458,14 @@ void tc_pack_weights(const float *w, void *out, cudaStream_t stream)
 void tc_conv(void *map_cache, const void *in, void *out, const void *wpacked, const float *bias, int nx, int ny, int nz,
              int batch, cudaStream_t stream, int *d_err)
 {
-    static const long long resident = [] {
+    static PerDevice<long long> setup;
+    const long long resident = setup.get([] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tc::conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
         int dev = 0, sms = 0;
         LGD_CHECK_CUDA(cudaGetDevice(&dev));
         LGD_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         return (long long)sms;
-    }();
+    });
     (void)map_cache;
     // z chunks: whole waves of one CTA per SM
     const long long xy = (long long)(nx / tc::TXO) * (ny / tc::TYO) * batch;

@@ -38,29 +38,39 @@ struct Jacobi7F32 {
 };
 
 // Jacobi-7 on the 64-bit fixed-point image of an FP64 grid (see
-// fx_div7_round): the neighbour sum is exact, the only rounding is the final
-// division, at most half a unit of 2^(scale_exp - 60).
-struct Jacobi7Fix {
+// fx_mul7_round): the neighbour sum is exact, the only rounding is the final
+// multiplication by fl(1/7), at most half a unit of 2^(scale_exp - 56).
+// NONNEG: every value and the edge cell are >= 0 (the sum is, too), which
+// saves the sign handling; both forms give the same result there.
+template<bool NONNEG>
+struct Jacobi7FixT {
     typedef long long T;
     static __device__ __forceinline__ T apply(T c, T n, T s, T e, T w, T t, T b)
     {
-        return fx_div7_round(c + n + s + e + w + t + b);
+        const T sum = c + n + s + e + w + t + b;
+        return NONNEG ? fx_mul7_round_nonneg(sum) : fx_mul7_round(sum);
     }
 };
+typedef Jacobi7FixT<false> Jacobi7Fix;
+typedef Jacobi7FixT<true> Jacobi7FixNonNeg;
 
 // Two Jacobi-7 steps in one pass with one rounding (the temporally blocked
 // fixed-point pass): the first level keeps the exact neighbour sum (7 times
-// the average), the second sums those and divides by 49.  The result is
-// round(exact two-step average), within one unit of two rounded single
-// steps.
-struct Jacobi7FixTwoStep {
+// the average), the second sums those and multiplies by fl(1/7)^2.  The
+// result is the rounded exact two-step product, within one unit of two
+// rounded single steps.
+template<bool NONNEG>
+struct Jacobi7FixTwoStepT {
     typedef long long T;
     static __device__ __forceinline__ T inner(T c, T n, T s, T e, T w, T t, T b) { return c + n + s + e + w + t + b; }
     static __device__ __forceinline__ T last(T c, T n, T s, T e, T w, T t, T b)
     {
-        return fx_div49_round(c + n + s + e + w + t + b);
+        const T sum = c + n + s + e + w + t + b;
+        return NONNEG ? fx_mul49_round_nonneg(sum) : fx_mul49_round(sum);
     }
 };
+typedef Jacobi7FixTwoStepT<false> Jacobi7FixTwoStep;
+typedef Jacobi7FixTwoStepT<true> Jacobi7FixTwoStepNonNeg;
 
 // Variable-coefficient diffusion: u' = u + sum over faces (-x, +x, -y, +y,
 // -z, +z) of 0.5 (k + k_nb)(u_nb - u).

@@ -60,36 +60,57 @@ __host__ __device__ __forceinline__ double splitmix_uniform(uint64_t key, uint64
 
 // ---- fixed-point representation of the FP64 Jacobi grid
 // value = k * 2^(scale_exp - LGD_FIX_BITS), k a signed 64-bit integer,
-// |value| < 2^scale_exp, so |k| < 2^56.  The averaging stencil maps
-// [-S, S] into itself, so 7 * 2^56 bounds every neighbour sum, and 49 * 2^56
-// < 2^62 every exact two-step sum (the temporally blocked pass): nothing
-// overflows.  56 fraction bits: each rounding adds at most 2^(scale_exp - 57),
-// e.g. 6.9e-18 for values in [0, 1).
-#define LGD_FIX_BITS 56
+// |value| < 2^scale_exp, so |k| < 2^57.  The averaging stencil maps
+// [-S, S] into itself, so 7 * 2^57 < 2^60 bounds every neighbour sum, and
+// 49 * 2^57 < 2^63 every exact two-step sum (the temporally blocked pass):
+// nothing overflows.  57 fraction bits: each rounding adds at most
+// 2^(scale_exp - 58), e.g. 3.5e-18 for values in [0, 1).
+#define LGD_FIX_BITS 57
 
-__device__ __forceinline__ long long fx_div7_round(long long sum)
+// The cell multiplies its neighbour sum by the double nearest 1/7,
+// fl(1/7) = LGD_FIX_C7 * 2^-54 exactly (0x3FC2492492492492), which is
+// 5.55e-17 (relatively) below 1/7.  The fixed-point steps multiply the exact
+// sum by that same constant, so they follow the reference's arithmetic
+// without the drift an exact division by 7 would accumulate against it
+// (1.1e-12 relative after 20,000 steps).
+//   single step: round(|sum| * fl(1/7)) = (hi64(|sum| * M7) + 1) >> 1 with
+//     M7 = fl(1/7) * 2^65 = LGD_FIX_C7 << 11 (exact, below 2^63): the +1 in
+//     the high word is the half unit, and the low word cannot carry into
+//     the result because it is below 2^64 = half of 2^65;
+//   two steps (exact sum of exact sums): round(|sum| * fl(1/7)^2) =
+//     (hi64(|sum| * M49) + 16) >> 5 with M49 = fl(1/7)^2 * 2^69 rounded to
+//     an integer (relative error below 2^-64: the product differs from the
+//     exact one by less than 0.006 units for |sum| < 49 * 2^57).
+// Rounding is to nearest, ties away from zero, and symmetric in the sign
+// like an IEEE multiplication.
+#define LGD_FIX_C7 2573485501354569ull
+#define LGD_FIX_M7 0x4924924924924800ull
+#define LGD_FIX_M49 0xa72f05397829c688ull
+
+// 0 <= sum < 7 * 2^57
+__device__ __forceinline__ long long fx_mul7_round_nonneg(long long sum)
 {
-    // round(sum / 7) (no ties exist), via an unsigned offset so that the
-    // division is one multiply-high: for n < 7 * 2^57 + 3 (and far beyond),
-    // floor(n / 7) = floor(n * ceil(2^65 / 7) / 2^65) exactly (the error
-    // term n * (3/7) / 2^65 stays below 1/7)
-    const unsigned long long off = 7ull << LGD_FIX_BITS;
-    const unsigned long long n = (unsigned long long)(sum + 3) + off;
-    const unsigned long long q = __umul64hi(n, 0x4924924924924925ull) >> 1;
-    return (long long)(q - (1ull << LGD_FIX_BITS));
+    return (long long)((__umul64hi((unsigned long long)sum, LGD_FIX_M7) + 1ull) >> 1);
 }
 
-__device__ __forceinline__ long long fx_div49_round(long long sum)
+__device__ __forceinline__ long long fx_mul7_round(long long sum)
 {
-    // round(sum / 49) for |sum| < 49 * 2^56 (no ties: sum + 24 is never a
-    // multiple of 49 plus a half).  n = sum + 24 + 49 * 2^56 < 98 * 2^56 + 25;
-    // floor(n / 49) = floor(n * M / 2^69), M = ceil(2^69 / 49): with
-    // M * 49 - 2^69 = 34, the error term n * 34 / (49 * 2^69) stays below
-    // 1/49 for n < 2^69 / 34
-    const unsigned long long off = 49ull << LGD_FIX_BITS;
-    const unsigned long long n = (unsigned long long)(sum + 24) + off;
-    const unsigned long long q = __umul64hi(n, 0xa72f05397829cbc2ull) >> 5;
-    return (long long)(q - (1ull << LGD_FIX_BITS));
+    const long long s = sum >> 63;                    // 0 or -1
+    const long long q = fx_mul7_round_nonneg((sum ^ s) - s);
+    return (q ^ s) - s;
+}
+
+// 0 <= sum < 49 * 2^57
+__device__ __forceinline__ long long fx_mul49_round_nonneg(long long sum)
+{
+    return (long long)((__umul64hi((unsigned long long)sum, LGD_FIX_M49) + 16ull) >> 5);
+}
+
+__device__ __forceinline__ long long fx_mul49_round(long long sum)
+{
+    const long long s = sum >> 63;
+    const long long q = fx_mul49_round_nonneg((sum ^ s) - s);
+    return (q ^ s) - s;
 }
 
 }  // namespace lgd

@@ -303,13 +303,13 @@ bool gol_tb_applicable(const Grid& g)
 // generation per pass), 1 = twice as tall, 2 = half as tall
 static int sm_count()
 {
-    static const int sms = [] {
+    static PerDevice<int> setup;
+    return setup.get([] {
         int dev = 0, count = 0;
         LGD_CHECK_CUDA(cudaGetDevice(&dev));
         LGD_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
         return count;
-    }();
-    return sms;
+    });
 }
 
 // resident CTAs per SM of a pass kernel, queried once (the query also
@@ -317,12 +317,12 @@ static int sm_count()
 template<int T>
 static int gol_tb_per_sm()
 {
-    static const int per_sm = [] {
+    static PerDevice<int> setup;
+    return setup.get([] {
         int n = 0;
         LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gol_tb_kernel<T>, 128, 0));
         return std::max(1, n);
-    }();
-    return per_sm;
+    });
 }
 
 template<int T>
@@ -354,12 +354,12 @@ constexpr int GOL_BITS_WPB = 4;                             // warps per CTA of 
 template<int T>
 static int gol_bits_per_sm()
 {
-    static const int per_sm = [] {
+    static PerDevice<int> setup;
+    return setup.get([] {
         int n = 0;
         LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gol_bits_kernel<T>, 32 * GOL_BITS_WPB, 0));
         return std::max(1, n);
-    }();
-    return per_sm;
+    });
 }
 
 // one bit-sliced pass of `depth` generations (2, 4, 6, 8, 12, 16, 24, 32
@@ -421,8 +421,8 @@ static int gol_tb_pass(Grid& g, int depth, int shape)
 // module load and no occupancy query inside the timed steps
 static void prepare_gol_kernels()
 {
-    static std::once_flag once;
-    std::call_once(once, [] {
+    static PerDevice<bool> setup;
+    setup.get([] {
         (void)sm_count();
         (void)gol_bits_per_sm<2>();
         (void)gol_bits_per_sm<4>();
@@ -440,6 +440,7 @@ static void prepare_gol_kernels()
         cudaFuncAttributes attr;
         LGD_CHECK_CUDA(cudaFuncGetAttributes(&attr, gol_swar_torus_kernel));
         LGD_CHECK_CUDA(cudaFuncGetAttributes(&attr, gol_generic_kernel));
+        return true;
     });
 }
 

@@ -282,6 +282,28 @@ void launch_region(Grid& g, const int *d_streaks, const long long *d_prefix, int
 }
 
 // ------------------------------------------------------------ streak copy
+// records of any size (record grids): one thread per record, 4-byte words
+// where the record size allows, else bytes
+template<typename W>
+__global__ void streak_copy_records_kernel(unsigned char *base, long pitch_bytes, int ny, int rec_words,
+                                           const int *streaks, const long long *prefix, int n_streaks,
+                                           long long cells, W *packed, bool to_grid)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= cells) return;
+    int x, y, z;
+    locate_cell(streaks, prefix, n_streaks, i, &x, &y, &z);
+    W *cell = (W *)(base + ((long)z * ny + y) * pitch_bytes) + (long)x * rec_words;
+    W *pk = packed + i * rec_words;
+    for (int k = 0; k < rec_words; ++k) {
+        if (to_grid) {
+            cell[k] = pk[k];
+        } else {
+            pk[k] = cell[k];
+        }
+    }
+}
+
 template<typename T>
 __global__ void streak_copy_kernel(View<T> v, const int *streaks, const long long *prefix, int n_streaks,
                                    long long cells, T *packed, bool to_grid)
@@ -320,8 +342,18 @@ void launch_streak_copy(Grid& g, int member, int which, const int *d_streaks, co
         streak_copy_kernel<TestRec><<<(unsigned)blocks, threads, 0, g.stream>>>(
             view_of<TestRec>(g, member, which), d_streaks, d_prefix, n_streaks, cells, (TestRec *)d_packed, to_grid);
         break;
-    default:
-        throw Error(LGD_ERR_INVALID, "unsupported member size");
+    default: {
+        const int elem = g.m[member].elem;
+        unsigned char *base = (unsigned char *)g.m[member].buf[g.m[member].is_static ? 0 : (which ? 1 - g.cur : g.cur)];
+        const long pitch = (long)g.pitch_bytes[member];
+        if (elem % 4 == 0) {
+            streak_copy_records_kernel<uint32_t><<<(unsigned)blocks, threads, 0, g.stream>>>(
+                base, pitch, g.desc.ny, elem / 4, d_streaks, d_prefix, n_streaks, cells, (uint32_t *)d_packed, to_grid);
+        } else {
+            streak_copy_records_kernel<uint8_t><<<(unsigned)blocks, threads, 0, g.stream>>>(
+                base, pitch, g.desc.ny, elem, d_streaks, d_prefix, n_streaks, cells, (uint8_t *)d_packed, to_grid);
+        }
+    }
     }
     check_launch("streak copy");
     ++g.launches;

@@ -112,13 +112,14 @@ struct TBOps<Jacobi7F32> {
     }
 };
 
-template<>
-struct TBOps<Jacobi7FixTwoStep> {
+template<bool NONNEG>
+struct TBOps<Jacobi7FixTwoStepT<NONNEG> > {
     typedef long long T;
+    typedef Jacobi7FixTwoStepT<NONNEG> C;
     static constexpr bool INTERIOR_PATH = true;
     static __device__ __forceinline__ T level(bool last, T c, T n, T s, T e, T w, T t, T b)
     {
-        return last ? Jacobi7FixTwoStep::last(c, n, s, e, w, t, b) : Jacobi7FixTwoStep::inner(c, n, s, e, w, t, b);
+        return last ? C::last(c, n, s, e, w, t, b) : C::inner(c, n, s, e, w, t, b);
     }
     static __device__ __forceinline__ void pair(bool last, T c0, T c1, T n0, T n1, T s0, T s1, T e0, T e1, T w0, T w1,
                                                 T t0, T t1, T b0, T b1, T& r0, T& r1)
@@ -320,12 +321,12 @@ template<typename CELL, int TB, int WY, int ROWS>
 static long long tb_resident()
 {
     typedef tbk::Geo<typename CELL::T, TB, WY, ROWS> G;
-    static const long long resident = [] {
+    static PerDevice<long long> setup;
+    return setup.get([] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
         return resident_ctas_tb((const void *)tbk::jacobi7_tb_kernel<CELL, TB, WY, ROWS>, G::THREADS, G::SMEM);
-    }();
-    return resident;
+    });
 }
 
 // Planes per CTA: minimise waves of resident CTAs times input planes per CTA
@@ -412,11 +413,14 @@ int tb_default_depth(const Grid& g)
 // every pass kernel set up once, on the first pass of any grid
 static void prepare_tb_kernels()
 {
-    static std::once_flag once;
-    std::call_once(once, [] {
+    static PerDevice<bool> setup;
+    setup.get([] {
         (void)tb_resident<Jacobi7FixTwoStep, 2, 16, 4>();
         (void)tb_resident<Jacobi7FixTwoStep, 2, 8, 4>();
         (void)tb_resident<Jacobi7FixTwoStep, 2, 16, 2>();
+        (void)tb_resident<Jacobi7FixTwoStepNonNeg, 2, 16, 4>();
+        (void)tb_resident<Jacobi7FixTwoStepNonNeg, 2, 8, 4>();
+        (void)tb_resident<Jacobi7FixTwoStepNonNeg, 2, 16, 2>();
         (void)tb_resident<Jacobi7F32, 2, 8, 4>();
         (void)tb_resident<Jacobi7F32, 2, 16, 4>();
         (void)tb_resident<Jacobi7F32, 2, 16, 2>();
@@ -426,6 +430,7 @@ static void prepare_tb_kernels()
         (void)tb_resident<Jacobi7F32, 4, 16, 4>();
         (void)tb_resident<Jacobi7F32, 4, 8, 4>();
         (void)tb_resident<Jacobi7F32, 4, 16, 2>();
+        return true;
     });
 }
 
@@ -436,10 +441,19 @@ void launch_jacobi7_tb(Grid& g, int depth, int shape)
     const int f32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     if (g.desc.cell == LGD_CELL_JACOBI7_F64_FIX) {
         LGD_REQUIRE(depth == 2, LGD_ERR_INVALID, "the fixed-point cell fuses two steps per pass");
-        switch (shape) {
-        case 1: launch_tb_typed<Jacobi7FixTwoStep, 2, 8, 4>(g, i64); break;
-        case 2: launch_tb_typed<Jacobi7FixTwoStep, 2, 16, 2>(g, i64); break;
-        default: launch_tb_typed<Jacobi7FixTwoStep, 2, 16, 4>(g, i64); break;
+        // grids without negative values skip the sign handling (same results)
+        if (g.fix_nonneg) {
+            switch (shape) {
+            case 1: launch_tb_typed<Jacobi7FixTwoStepNonNeg, 2, 8, 4>(g, i64); break;
+            case 2: launch_tb_typed<Jacobi7FixTwoStepNonNeg, 2, 16, 2>(g, i64); break;
+            default: launch_tb_typed<Jacobi7FixTwoStepNonNeg, 2, 16, 4>(g, i64); break;
+            }
+        } else {
+            switch (shape) {
+            case 1: launch_tb_typed<Jacobi7FixTwoStep, 2, 8, 4>(g, i64); break;
+            case 2: launch_tb_typed<Jacobi7FixTwoStep, 2, 16, 2>(g, i64); break;
+            default: launch_tb_typed<Jacobi7FixTwoStep, 2, 16, 4>(g, i64); break;
+            }
         }
     } else if (g.desc.cell == LGD_CELL_JACOBI7_F32) {
         switch (depth * 10 + shape) {
@@ -466,7 +480,7 @@ void launch_jacobi7_tb(Grid& g, int depth, int shape)
 }
 
 // Deepest Jacobi pass of a cell: the fixed-point cell's exact two-step sums
-// stay below 2^63 (49 * 2^56), deeper fusion would need fewer fraction bits;
+// stay below 2^63 (49 * 2^57), deeper fusion would need fewer fraction bits;
 // the FP32 kernel is instantiated up to 4.
 int tb_max_depth(const Grid& g)
 {

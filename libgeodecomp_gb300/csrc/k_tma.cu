@@ -55,10 +55,14 @@ struct Box {
     static constexpr int SLOT = (BYTES + 127) / 128 * 128;
 };
 
+// wait_cycles bounds every mbarrier wait; skip_plane >= 0 (tests of the
+// timeout path only, lgd_gpu_test_bounded_waits) makes CTA (0, 0, 0) leave
+// that plane's copy unissued, so the wait for it runs out: the CTA sets the
+// error word, drains the copies it did issue and returns
 template<typename CELL>
 __global__ void __launch_bounds__(THREADS)
 jacobi7_tma_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T *__restrict__ out, long pitch, int nx,
-                   int ny, int nz, int zchunk, int *err)
+                   int ny, int nz, int zchunk, int *err, long long wait_cycles, int skip_plane)
 {
     typedef typename CELL::T T;
     typedef Box<T> B;
@@ -77,12 +81,14 @@ jacobi7_tma_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T 
     if (z0 >= z1) return;                       // uniform across the CTA
     const int nplanes = (z1 - z0) + 2;          // plane q is z = z0 - 1 + q
 
+    const int skip = (blockIdx.x | blockIdx.y | blockIdx.z) == 0 ? skip_plane : -1;
     if (tid == 0) {
         for (int s = 0; s < S; ++s) mbar_init(smem_addr(&bars[s]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_fail = 0;
         const int first = min(D, nplanes - 1);
         for (int q = 0; q <= first; ++q) {
+            if (q == skip) continue;
             const uint32_t bar = smem_addr(&bars[q % S]);
             mbar_expect_tx(bar, B::BYTES);
             tma_load_3d(smem_addr(smem + (q % S) * B::SLOT), &in_map, x0 - B::XPAD, y0 - 1, z0 - 1 + q, bar);
@@ -93,7 +99,7 @@ jacobi7_tma_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T 
 
     int waited = -1;    // highest plane this thread has waited for
     for (int q = 0; q < 2; ++q) {
-        if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1)) s_fail = 1;
+        if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1, wait_cycles)) s_fail = 1;
         waited = q;
     }
 
@@ -108,12 +114,14 @@ jacobi7_tma_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T 
         if (s_fail) break;                      // uniform: read after the barrier
         if (tid == 0 && q + D < nplanes) {
             const int qn = q + D;
-            const uint32_t bar = smem_addr(&bars[qn % S]);
-            mbar_expect_tx(bar, B::BYTES);
-            tma_load_3d(smem_addr(smem + (qn % S) * B::SLOT), &in_map, x0 - B::XPAD, y0 - 1, z0 - 1 + qn, bar);
+            if (qn != skip) {
+                const uint32_t bar = smem_addr(&bars[qn % S]);
+                mbar_expect_tx(bar, B::BYTES);
+                tma_load_3d(smem_addr(smem + (qn % S) * B::SLOT), &in_map, x0 - B::XPAD, y0 - 1, z0 - 1 + qn, bar);
+            }
             s_issued = qn + 1;
         }
-        if (!mbar_wait_bounded(smem_addr(&bars[(q + 1) % S]), ((q + 1) / S) & 1)) {
+        if (!mbar_wait_bounded(smem_addr(&bars[(q + 1) % S]), ((q + 1) / S) & 1, wait_cycles)) {
             s_fail = 1;
             continue;
         }
@@ -167,7 +175,8 @@ jacobi7_tma_kernel(const __grid_constant__ CUtensorMap in_map, typename CELL::T 
         // the shared memory is released
         if (tid == 0) atomicExch(err, 1);
         for (int q = waited + 1; q < s_issued; ++q) {
-            if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1)) break;
+            if (q == skip) continue;            // never issued
+            if (!mbar_wait_bounded(smem_addr(&bars[q % S]), (q / S) & 1, wait_cycles)) break;
         }
     }
 }
@@ -496,12 +505,12 @@ static void launch_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.tmap_base[src] = g.m[0].buf[src];
     }
     const int smem = tmak::S * tmak::Box<T>::SLOT;
-    static const bool configured = [smem] {
+    static PerDevice<bool> setup;
+    setup.get([smem] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::jacobi7_tma_kernel<CELL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             smem));
         return true;
-    }();
-    (void)configured;
+    });
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
     const long long xy = (long long)bx * by;
@@ -517,7 +526,7 @@ static void launch_tma_typed(Grid& g, CUtensorMapDataType dt)
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(g.tmap[src]);
     tmak::jacobi7_tma_kernel<CELL><<<dim3(bx, by, zsplit), tmak::THREADS, smem, g.stream>>>(
         *map, (T *)g.m[0].buf[1 - src], (long)(g.pitch_bytes[0] / sizeof(T)), g.desc.nx, g.desc.ny, g.desc.nz, zchunk,
-        g.d_err);
+        g.d_err, g.test_wait_cycles > 0 ? g.test_wait_cycles : tmak::WAIT_CYCLES, g.test_skip_plane - 1);
 }
 
 // The var-coef TMA kernel: 3D grids whose non-wrapping axes have zero edge
@@ -553,10 +562,11 @@ static void launch_varcoef_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.vtmap_base[src][1] = kbuf;
     }
     const int smem = tmak::VC_S * tmak::vc::Lay<R>::SLOT;
-    static const long long resident = [smem] {
+    static PerDevice<long long> setup;
+    const long long resident = setup.get([smem] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::varcoef_tma_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         return tmak::resident_ctas((const void *)tmak::varcoef_tma_kernel<R>, tmak::THREADS, smem);
-    }();
+    });
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
     const int zchunk = tmak::pick_zchunk((long long)bx * by, g.desc.nz, resident);
@@ -588,7 +598,12 @@ void launch_jacobi7_tma(Grid& g)
         launch_tma_typed<Jacobi7F32>(g, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
         break;
     case LGD_CELL_JACOBI7_F64_FIX:
-        launch_tma_typed<Jacobi7Fix>(g, CU_TENSOR_MAP_DATA_TYPE_INT64);
+        // grids without negative values skip the sign handling (same results)
+        if (g.fix_nonneg) {
+            launch_tma_typed<Jacobi7FixNonNeg>(g, CU_TENSOR_MAP_DATA_TYPE_INT64);
+        } else {
+            launch_tma_typed<Jacobi7Fix>(g, CU_TENSOR_MAP_DATA_TYPE_INT64);
+        }
         break;
     default:
         throw Error(LGD_ERR_UNSUPPORTED, "not a Jacobi cell");

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -58,6 +59,34 @@ int guard(F&& f)
     }
 }
 
+// A value set up once per device, with that device current: kernel
+// attributes (the dynamic shared-memory limit), occupancy and SM counts
+// apply per device, so a process that drives several GPUs sets each up on
+// its first use there.
+template<typename T>
+class PerDevice {
+public:
+    template<typename F>
+    T get(F&& init)
+    {
+        int dev = 0;
+        LGD_CHECK_CUDA(cudaGetDevice(&dev));
+        LGD_REQUIRE(dev >= 0 && dev < MAX_DEVICES, LGD_ERR_UNSUPPORTED, "device index above 63");
+        std::lock_guard<std::mutex> lock(mutex);
+        if (!ready[dev]) {
+            value[dev] = init();
+            ready[dev] = true;
+        }
+        return value[dev];
+    }
+
+private:
+    static const int MAX_DEVICES = 64;
+    std::mutex mutex;
+    T value[MAX_DEVICES] = {};
+    bool ready[MAX_DEVICES] = {};
+};
+
 // Throws if the last launch failed to start.
 inline void check_launch(const char *what)
 {
@@ -88,6 +117,12 @@ struct Grid {
     int time_block;         // temporal blocking depth (0 = default)
     int tb_shape;           // temporal blocking box shape (0 = default for the cell and depth)
     int fix_exp;            // fixed-point grids: value = k * 2^(fix_exp - LGD_FIX_BITS)
+    bool fix_nonneg;        // fixed-point grids: no negative value or edge cell so far
+    bool fix_pinned;        // fixed-point grids: the exponent is only raised, never lowered
+    int fix_steps_unchecked;    // fixed-point grids: steps since the exponent was last lowered
+    unsigned long long *d_fixmax;   // fixed-point grids: [0] max |k| of a check, [1] negative-value flag
+    unsigned char *edge_record;     // record grids: the edge cell (host copy, malloc'd)
+    void *d_edge_record;            // record grids: the edge cell on the device
     int variant;            // kernel variant where a cell has several (0 = default)
     cudaStream_t stream;
     uint64_t launches;
@@ -104,6 +139,11 @@ struct Grid {
     bool tmap_ready[2];
     void *tmap_base[2];
     int *d_err;
+    // tests of the timeout path (lgd_gpu_test_bounded_waits): wait bound of
+    // the TMA Jacobi kernel (0 = the default) and 1 + the plane whose copy
+    // its first CTA leaves unissued (0 = none)
+    long long test_wait_cycles;
+    int test_skip_plane;
     void *d_stage;          // conversion staging at the boundary (fixed-point grids)
     size_t stage_bytes;
     // fixed-point transfers in row chunks: copies on xfer_stream, the

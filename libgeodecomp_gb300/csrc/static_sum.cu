@@ -1,5 +1,7 @@
-// lgd_sum_f64_static: the FP64 sum of lgd_gpu_checksum for callers that
-// must not allocate device memory.
+// lgd_sum_f64_static: an FP64 sum for callers that must not allocate device
+// memory - the same sum as lgd_gpu_checksum, added in a different order
+// (blocks of 65536 values and a tree on the device), so not bit-identical
+// to it.
 //
 // Who needs it: code that runs inside another framework's stream and memory
 // pool - a Writer or Steerer plugin called in the middle of a simulation
@@ -67,27 +69,57 @@ static_sum_final_kernel(const double *__restrict__ partials, int count, double *
     if (threadIdx.x == 0) *out = red[0];
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current.  (In host code the array's name is only a host-side
-// stand-in: passing it to a kernel would reach the wrong memory.)
+// Device address of the scratch array, looked up once per device and
+// context with that device current.  (In host code the array's name is only
+// a host-side stand-in: passing it to a kernel would reach the wrong
+// memory.)  The cache is keyed on the device's current context as well:
+// after a cudaDeviceReset the primary context is created anew, the module
+// is loaded again and the array may move, so a new context means a new
+// lookup.  cudaGetSymbolAddress allocates nothing.
 static const int kMaxDevices = 64;
 static std::mutex g_scratch_mutex;
 static double *g_scratch_ptr[kMaxDevices];
+static void *g_scratch_ctx[kMaxDevices];
+
+typedef int (*CtxGetCurrentFn)(void **);
+
+// the driver's cuCtxGetCurrent, through the runtime's entry-point query
+static CtxGetCurrentFn ctx_get_current()
+{
+    static const CtxGetCurrentFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            p = nullptr;
+        }
+        return (CtxGetCurrentFn)p;
+    }();
+    return fn;
+}
 
 static double *scratch_for_current_device()
 {
     int dev = 0;
     LGD_CHECK_CUDA(cudaGetDevice(&dev));
     LGD_REQUIRE(dev >= 0 && dev < kMaxDevices, LGD_ERR_UNSUPPORTED, "device index above 63");
+    const CtxGetCurrentFn get = ctx_get_current();
+    LGD_REQUIRE(get != nullptr, LGD_ERR_CUDA, "cuCtxGetCurrent is not available");
+    void *ctx = nullptr;
+    if (get(&ctx) != 0) ctx = nullptr;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (ctx == nullptr || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
+        // (the lookup also makes the device's primary context current when
+        // no context is yet)
         double *ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_sum_scratch);
         if (e != cudaSuccess || ptr == nullptr) {
             throw Error(LGD_ERR_CUDA, std::string("cudaGetSymbolAddress of the sum scratch failed: ") +
                                           cudaGetErrorString(e));
         }
+        if (get(&ctx) != 0) ctx = nullptr;
         g_scratch_ptr[dev] = ptr;
+        g_scratch_ctx[dev] = ctx;
     }
     return g_scratch_ptr[dev];
 }

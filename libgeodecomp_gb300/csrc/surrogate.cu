@@ -582,12 +582,12 @@ template<int CIN, int COUT, int TX, int MODE, bool GIN = false>
 static void run_fwd(Net& n, const bf16 *in, const uint2 *frag, const float *bias, bf16 *oh, float *oz, float *of)
 {
     const size_t sm = fwd_smem<CIN, COUT, TX, MODE>();
-    static const bool configured = [sm] {     // per instantiation, per process
+    static PerDevice<bool> setup;             // per instantiation, per device
+    setup.get([sm] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, TX, MODE, GIN>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         return true;
-    }();
-    (void)configured;
+    });
     dim3 grid(n.g.nx / TX, n.g.ny / TYT, n.g.nz * n.g.batch);
     conv_fwd_kernel<CIN, COUT, TX, MODE, GIN><<<grid, THREADS, sm, n.stream>>>(in, frag, bias, n.g, oh, oz, of);
     check_launch("conv forward");
@@ -598,12 +598,12 @@ template<int CIN, int COUT, int TX>
 static void run_wgrad(Net& n, const bf16 *in, const bf16 *dz, float *dW)
 {
     const size_t sm = wgrad_smem<CIN, COUT, TX>();
-    static const bool configured = [sm] {
+    static PerDevice<bool> setup;
+    setup.get([sm] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(conv_wgrad_kernel<CIN, COUT, TX>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         return true;
-    }();
-    (void)configured;
+    });
     dim3 grid(n.g.nx / TX, n.g.ny / TYT, n.g.nz * n.g.batch);
     conv_wgrad_kernel<CIN, COUT, TX><<<grid, THREADS, sm, n.stream>>>(in, dz, n.g, dW);
     check_launch("conv weight gradient");

@@ -6,6 +6,7 @@
 // against either:
 //   Coord / CoordBox / Streak / Region      geometry/coord.h, coordbox.h,
 //                                           streak.h, region.h
+//   FixedCoord                              geometry/fixedcoord.h
 //   Topologies::Cube / Torus, WrapsAxis     geometry/topologies.h:179-278
 //   Stencils::Moore / VonNeumann            geometry/stencils.h:182-227
 //   APITraits (topology, nano steps, tags)  misc/apitraits.h:69-836
@@ -18,7 +19,11 @@
 //   Simulator, MonolithicSimulator          parallelization/simulator.h:28-106,
 //                                           parallelization/monolithicsimulator.h:16-52
 // Only what a single-node simulator needs is here: no MPI, no HPX, no
-// serialisation, no region algebra beyond streak lists.
+// serialisation, no region algebra beyond streak lists.  What a cell's
+// update() uses (Coord, FixedCoord, the topologies' normalize and
+// isOutOfBounds, the stencils' Coords and RepeatCuda) is callable on the
+// device when nvcc compiles it, as in the reference, so one cell source
+// runs on the host and, through gb300cell.cuh, on the GPU.
 #ifndef LGD_GB300_COMPAT_H
 #define LGD_GB300_COMPAT_H
 
@@ -30,11 +35,28 @@
 #include <string>
 #include <vector>
 
+#ifdef __CUDACC__
+#define LGD_COMPAT_HD __host__ __device__
+#else
+#define LGD_COMPAT_HD
+#endif
+
 namespace LibGeoDecomp {
 
 template<typename T>
 struct SharedPtr {
     typedef std::shared_ptr<T> Type;
+};
+
+// ------------------------------------------------------------- FixedCoord
+// A compile-time offset (the stencils' neighbour positions).
+template<int DIM_X = 0, int DIM_Y = 0, int DIM_Z = 0>
+class FixedCoord {
+public:
+    static const int X = DIM_X;
+    static const int Y = DIM_Y;
+    static const int Z = DIM_Z;
+    LGD_COMPAT_HD FixedCoord() {}
 };
 
 // ------------------------------------------------------------------ Coord
@@ -44,16 +66,18 @@ class Coord;
 template<>
 class Coord<1> {
 public:
-    explicit Coord(int x = 0) { c[0] = x; }
-    int x() const { return c[0]; }
-    int& operator[](int i) { return c[i]; }
-    int operator[](int i) const { return c[i]; }
-    long prod() const { return c[0]; }
-    bool operator==(const Coord& o) const { return c[0] == o.c[0]; }
-    bool operator!=(const Coord& o) const { return !(*this == o); }
-    Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0]); }
-    Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0]); }
-    static Coord diagonal(int v) { return Coord(v); }
+    LGD_COMPAT_HD explicit Coord(int x = 0) { c[0] = x; }
+    template<int X, int Y, int Z>
+    LGD_COMPAT_HD explicit Coord(FixedCoord<X, Y, Z>) { c[0] = X; }
+    LGD_COMPAT_HD int x() const { return c[0]; }
+    LGD_COMPAT_HD int& operator[](int i) { return c[i]; }
+    LGD_COMPAT_HD int operator[](int i) const { return c[i]; }
+    LGD_COMPAT_HD long prod() const { return c[0]; }
+    LGD_COMPAT_HD bool operator==(const Coord& o) const { return c[0] == o.c[0]; }
+    LGD_COMPAT_HD bool operator!=(const Coord& o) const { return !(*this == o); }
+    LGD_COMPAT_HD Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0]); }
+    LGD_COMPAT_HD Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0]); }
+    LGD_COMPAT_HD static Coord diagonal(int v) { return Coord(v); }
 
 private:
     int c[1];
@@ -62,17 +86,19 @@ private:
 template<>
 class Coord<2> {
 public:
-    explicit Coord(int x = 0, int y = 0) { c[0] = x; c[1] = y; }
-    int x() const { return c[0]; }
-    int y() const { return c[1]; }
-    int& operator[](int i) { return c[i]; }
-    int operator[](int i) const { return c[i]; }
-    long prod() const { return (long)c[0] * c[1]; }
-    bool operator==(const Coord& o) const { return c[0] == o.c[0] && c[1] == o.c[1]; }
-    bool operator!=(const Coord& o) const { return !(*this == o); }
-    Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0], c[1] + o.c[1]); }
-    Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0], c[1] - o.c[1]); }
-    static Coord diagonal(int v) { return Coord(v, v); }
+    LGD_COMPAT_HD explicit Coord(int x = 0, int y = 0) { c[0] = x; c[1] = y; }
+    template<int X, int Y, int Z>
+    LGD_COMPAT_HD explicit Coord(FixedCoord<X, Y, Z>) { c[0] = X; c[1] = Y; }
+    LGD_COMPAT_HD int x() const { return c[0]; }
+    LGD_COMPAT_HD int y() const { return c[1]; }
+    LGD_COMPAT_HD int& operator[](int i) { return c[i]; }
+    LGD_COMPAT_HD int operator[](int i) const { return c[i]; }
+    LGD_COMPAT_HD long prod() const { return (long)c[0] * c[1]; }
+    LGD_COMPAT_HD bool operator==(const Coord& o) const { return c[0] == o.c[0] && c[1] == o.c[1]; }
+    LGD_COMPAT_HD bool operator!=(const Coord& o) const { return !(*this == o); }
+    LGD_COMPAT_HD Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0], c[1] + o.c[1]); }
+    LGD_COMPAT_HD Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0], c[1] - o.c[1]); }
+    LGD_COMPAT_HD static Coord diagonal(int v) { return Coord(v, v); }
 
 private:
     int c[2];
@@ -81,18 +107,23 @@ private:
 template<>
 class Coord<3> {
 public:
-    explicit Coord(int x = 0, int y = 0, int z = 0) { c[0] = x; c[1] = y; c[2] = z; }
-    int x() const { return c[0]; }
-    int y() const { return c[1]; }
-    int z() const { return c[2]; }
-    int& operator[](int i) { return c[i]; }
-    int operator[](int i) const { return c[i]; }
-    long prod() const { return (long)c[0] * c[1] * c[2]; }
-    bool operator==(const Coord& o) const { return c[0] == o.c[0] && c[1] == o.c[1] && c[2] == o.c[2]; }
-    bool operator!=(const Coord& o) const { return !(*this == o); }
-    Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0], c[1] + o.c[1], c[2] + o.c[2]); }
-    Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0], c[1] - o.c[1], c[2] - o.c[2]); }
-    static Coord diagonal(int v) { return Coord(v, v, v); }
+    LGD_COMPAT_HD explicit Coord(int x = 0, int y = 0, int z = 0) { c[0] = x; c[1] = y; c[2] = z; }
+    template<int X, int Y, int Z>
+    LGD_COMPAT_HD explicit Coord(FixedCoord<X, Y, Z>) { c[0] = X; c[1] = Y; c[2] = Z; }
+    LGD_COMPAT_HD int x() const { return c[0]; }
+    LGD_COMPAT_HD int y() const { return c[1]; }
+    LGD_COMPAT_HD int z() const { return c[2]; }
+    LGD_COMPAT_HD int& operator[](int i) { return c[i]; }
+    LGD_COMPAT_HD int operator[](int i) const { return c[i]; }
+    LGD_COMPAT_HD long prod() const { return (long)c[0] * c[1] * c[2]; }
+    LGD_COMPAT_HD bool operator==(const Coord& o) const
+    {
+        return c[0] == o.c[0] && c[1] == o.c[1] && c[2] == o.c[2];
+    }
+    LGD_COMPAT_HD bool operator!=(const Coord& o) const { return !(*this == o); }
+    LGD_COMPAT_HD Coord operator+(const Coord& o) const { return Coord(c[0] + o.c[0], c[1] + o.c[1], c[2] + o.c[2]); }
+    LGD_COMPAT_HD Coord operator-(const Coord& o) const { return Coord(c[0] - o.c[0], c[1] - o.c[1], c[2] - o.c[2]); }
+    LGD_COMPAT_HD static Coord diagonal(int v) { return Coord(v, v, v); }
 
 private:
     int c[3];
@@ -220,12 +251,23 @@ public:
         static const bool VALUE = WRAP && (D < DIMENSIONS);
     };
 
-    static Coord<DIM> normalize(Coord<DIM> c, const Coord<DIM>& dim)
+    // wraps coordinates into the grid on periodic axes
+    LGD_COMPAT_HD static Coord<DIM> normalize(Coord<DIM> c, const Coord<DIM>& dim)
     {
         for (int d = 0; d < DIM; ++d) {
             if (WRAP) c[d] = ((c[d] % dim[d]) + dim[d]) % dim[d];
         }
         return c;
+    }
+
+    // outside the grid on a non-periodic axis (the edge cell's positions)
+    LGD_COMPAT_HD static bool isOutOfBounds(const Coord<DIM>& c, const Coord<DIM>& dim)
+    {
+        bool out = false;
+        for (int d = 0; d < DIM; ++d) {
+            out |= !WRAP && (c[d] < 0 || c[d] >= dim[d]);
+        }
+        return out;
     }
 };
 
@@ -254,20 +296,70 @@ constexpr int vonNeumannVolume(int d, int r)
 }
 constexpr int mooreVolume(int d, int r) { return d == 0 ? 1 : (2 * r + 1) * mooreVolume(d - 1, r); }
 
-template<int DIM, int RADIUS>
+// Offset `axis` of the index-th point of a stencil: the points of the
+// (2r + 1)^d box in x-fastest order (the reference's Moore order), keeping
+// only |x| + |y| + |z| <= r for von Neumann stencils.
+constexpr int stencilOffset(int dim, int r, bool diamond, int index, int axis)
+{
+    const int w = 2 * r + 1;
+    const int box = mooreVolume(dim, r);
+    int seen = -1;
+    for (int i = 0; i < box; ++i) {
+        const int x = i % w - r;
+        const int y = dim > 1 ? (i / w) % w - r : 0;
+        const int z = dim > 2 ? i / (w * w) - r : 0;
+        const int l1 = (x < 0 ? -x : x) + (y < 0 ? -y : y) + (z < 0 ? -z : z);
+        if (diamond && l1 > r) continue;
+        if (++seen == index) return axis == 0 ? x : axis == 1 ? y : z;
+    }
+    return 0;
+}
+
+template<int DIMENSIONS, int RAD>
 class VonNeumann {
 public:
-    static const int DIMENSIONS = DIM;
-    static const int RADIUS_ = RADIUS;
-    static const int VOLUME = vonNeumannVolume(DIM, RADIUS);
+    static const int DIM = DIMENSIONS;
+    static const int RADIUS = RAD;
+    static const int VOLUME = vonNeumannVolume(DIMENSIONS, RAD);
+    template<int INDEX>
+    class Coords : public FixedCoord<stencilOffset(DIMENSIONS, RAD, true, INDEX, 0),
+                                     stencilOffset(DIMENSIONS, RAD, true, INDEX, 1),
+                                     stencilOffset(DIMENSIONS, RAD, true, INDEX, 2)> {};
 };
-template<int DIM, int RADIUS>
+
+template<int DIMENSIONS, int RAD>
 class Moore {
 public:
-    static const int DIMENSIONS = DIM;
-    static const int RADIUS_ = RADIUS;
-    static const int VOLUME = mooreVolume(DIM, RADIUS);
+    static const int DIM = DIMENSIONS;
+    static const int RADIUS = RAD;
+    static const int VOLUME = mooreVolume(DIMENSIONS, RAD);
+    template<int INDEX>
+    class Coords : public FixedCoord<stencilOffset(DIMENSIONS, RAD, false, INDEX, 0),
+                                     stencilOffset(DIMENSIONS, RAD, false, INDEX, 1),
+                                     stencilOffset(DIMENSIONS, RAD, false, INDEX, 2)> {};
 };
+
+// TEMPLATE<PARAM, I>()(cargo...) for I = 0 .. NUM - 1, on host and device
+template<int NUM, template<class C, int I> class TEMPLATE, class PARAM>
+class RepeatCuda {
+public:
+    template<typename... CARGO>
+    LGD_COMPAT_HD void operator()(CARGO... cargo) const
+    {
+        RepeatCuda<NUM - 1, TEMPLATE, PARAM>()(cargo...);
+        TEMPLATE<PARAM, NUM - 1>()(cargo...);
+    }
+};
+
+template<template<class C, int I> class TEMPLATE, class PARAM>
+class RepeatCuda<0, TEMPLATE, PARAM> {
+public:
+    template<typename... CARGO>
+    LGD_COMPAT_HD void operator()(CARGO...) const {}
+};
+
+template<int NUM, template<class C, int I> class TEMPLATE, class PARAM>
+class Repeat : public RepeatCuda<NUM, TEMPLATE, PARAM> {};
 }  // namespace Stencils
 
 // -------------------------------------------------------------- APITraits
@@ -334,6 +426,28 @@ public:
     class SelectStencil<CELL, typename CELL::API::SupportsStencil> {
     public:
         typedef typename CELL::API::Stencil Value;
+    };
+
+    class TrueType {};
+    class FalseType {};
+
+    // a cell with this trait runs updateCUDA() instead of update() on the
+    // device (misc/apitraits.h:814-836)
+    class HasSeparateCUDAUpdate {
+    public:
+        typedef void SupportsSeparateCUDAUpdate;
+    };
+
+    template<typename CELL, typename HAS = void>
+    class SelectSeparateCUDAUpdate {
+    public:
+        typedef FalseType Value;
+    };
+
+    template<typename CELL>
+    class SelectSeparateCUDAUpdate<CELL, typename CELL::API::SupportsSeparateCUDAUpdate> {
+    public:
+        typedef TrueType Value;
     };
 
     class HasSoA {};

@@ -28,9 +28,15 @@
 //     call (which may fuse them into fewer passes over memory); the plugin
 //     calls themselves are unchanged.
 //
-// Cells are bound to a kernel compiled into the library by specialising
-// GB300CellTraits<CELL> (see below); the cell class and its API traits stay
-// as they are.
+// A cell runs on the device in one of two ways; the cell class and its API
+// traits stay as they are either way:
+//   - bound to a kernel compiled into the library by specialising
+//     GB300CellTraits<CELL> (see below): the fast paths (TMA plane rings,
+//     temporal blocking), for the cells the library restates;
+//   - any other cell runs its own update() / updateCUDA() on the device, as
+//     under the reference's CUDASimulator: the translation unit includes
+//     gb300cell.cuh and is compiled by nvcc; the grid is a record grid
+//     (LGD_CELL_RECORD, one sizeof(CELL) record per cell).
 //
 // Build with -DLGD_GB300_WITH_REFERENCE and the reference's include paths to
 // plug into a LibGeoDecomp application; without it the declarations in
@@ -67,8 +73,31 @@ namespace LibGeoDecomp {
 //   static void pack(const CELL& c, int m, void *dst);     member m -> dst
 //   static void unpack(CELL *c, int m, const void *src);   src -> member m
 //   static double edgeValue(const CELL& c, int m);         member m as double
+// Without a specialisation the cell is a record cell: its grid holds the
+// CELL objects themselves and its own update() runs on the device
+// (gb300cell.cuh).
 template<typename CELL>
-class GB300CellTraits;
+class GB300CellTraits {
+public:
+    static const int KIND = LGD_CELL_RECORD;
+    static const int MEMBERS = 1;
+    static std::size_t memberSize(int) { return sizeof(CELL); }
+    static void pack(const CELL& c, int, void *dst) { std::memcpy(dst, static_cast<const void *>(&c), sizeof(CELL)); }
+    static void unpack(CELL *c, int, const void *src) { std::memcpy(static_cast<void *>(c), src, sizeof(CELL)); }
+    static double edgeValue(const CELL&, int) { return 0.0; }
+};
+
+// Advances a device grid: compiled kinds through lgd_gpu_step; record cells
+// through their own update() in a kernel that gb300cell.cuh defines (a
+// translation unit with a record cell must include it and be compiled by
+// nvcc; otherwise GB300DeviceStep<CELL, true> stays incomplete).
+template<typename CELL, bool RECORD = (GB300CellTraits<CELL>::KIND == LGD_CELL_RECORD)>
+struct GB300DeviceStep {
+    static void run(lgd_handle *h, unsigned nanoStep, int count);
+};
+
+template<typename CELL>
+struct GB300DeviceStep<CELL, true>;
 
 // Optional in a binding: static int descFlags() - the grid descriptor's
 // flags (cell kinds that take some, LGD_CELL_TEST); 0 when absent.
@@ -157,6 +186,12 @@ inline void gb300Check(int rc)
     default:
         throw std::runtime_error(std::string("CUDA error: ") + msg);
     }
+}
+
+template<typename CELL, bool RECORD>
+void GB300DeviceStep<CELL, RECORD>::run(lgd_handle *h, unsigned nanoStep, int count)
+{
+    gb300Check(lgd_gpu_step(h, nanoStep, count));
 }
 
 // Read-only view of the device grid handed to Writers.  A Writer that
@@ -279,18 +314,17 @@ private:
             gb300Check(lgd_gpu_save_region(*handle, m, streaks.data(), rows, bufs[m].data(), bufs[m].size()));
             fetched += bufs[m].size();
         }
+        // rows are contiguous along x in the host grid
         std::size_t i = 0;
         for (int y = y0; y < y1; ++y) {
+            Coord<DIM> c = box.origin;
+            if (DIM > 1) c[1] += y;
+            if (DIM > 2) c[2] += z;
+            CELL *row = &(*grid)[c];
             for (int x = 0; x < nx; ++x, ++i) {
-                Coord<DIM> c = box.origin;
-                c[0] += x;
-                if (DIM > 1) c[1] += y;
-                if (DIM > 2) c[2] += z;
-                CELL cell = grid->get(c);
                 for (int m = 0; m < Traits::MEMBERS; ++m) {
-                    Traits::unpack(&cell, m, &bufs[m][i * Traits::memberSize(m)]);
+                    Traits::unpack(&row[x], m, &bufs[m][i * Traits::memberSize(m)]);
                 }
-                grid->set(c, cell);
             }
         }
         valid[p] = 1;
@@ -356,7 +390,7 @@ public:
             // compute time includes the device's: the scope waits for it
             TimeCompute t(&this->chronometer);
             for (unsigned i = 0; i < NANO_STEPS; ++i) {
-                gb300Check(lgd_gpu_step(handle, i, 1));
+                GB300DeviceStep<CELL>::run(handle, i, 1);
             }
             gb300Check(lgd_gpu_synchronize(handle));
         }
@@ -376,9 +410,14 @@ public:
         view->markAllValid();
         this->stepNum = this->initializer->startStep();
         if (edgeChanged()) {
-            gb300Check(lgd_gpu_destroy(handle));
-            handle = 0;
-            createDevice();
+            if (Traits::KIND == LGD_CELL_RECORD) {
+                gb300Check(lgd_gpu_set_edge_record(handle, &hostGrid->getEdge(), sizeof(CELL)));
+                std::memcpy(edgeRecord.data(), static_cast<const void *>(&hostGrid->getEdge()), sizeof(CELL));
+            } else {
+                gb300Check(lgd_gpu_destroy(handle));
+                handle = 0;
+                createDevice();
+            }
         }
         upload();
         for (std::size_t i = 0; i < this->steerers.size(); ++i) {
@@ -416,6 +455,7 @@ private:
     CoordBox<DIM> box;
     Region<DIM> simArea;
     double edge[4];
+    std::vector<unsigned char> edgeRecord;      // record cells: the edge cell's bytes
 
     void createDevice()
     {
@@ -430,32 +470,68 @@ private:
                      (Topology::template WrapsAxis<2>::VALUE ? 4 : 0);
         d.cell = Traits::KIND;
         d.flags = GB300DescFlags<Traits>::value();
-        for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
-            d.edge[m] = Traits::edgeValue(hostGrid->getEdge(), m);
-            edge[m] = d.edge[m];
+        if (Traits::KIND == LGD_CELL_RECORD) {
+            const CELL& e = hostGrid->getEdge();
+            edgeRecord.resize(sizeof(CELL));
+            std::memcpy(edgeRecord.data(), static_cast<const void *>(&e), sizeof(CELL));
+            gb300Check(lgd_gpu_create_records(&d, sizeof(CELL), edgeRecord.data(), &handle));
+        } else {
+            for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
+                d.edge[m] = Traits::edgeValue(hostGrid->getEdge(), m);
+                edge[m] = d.edge[m];
+            }
+            gb300Check(lgd_gpu_create(&d, &handle));
         }
-        gb300Check(lgd_gpu_create(&d, &handle));
     }
 
     bool edgeChanged() const
     {
-        for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
-            if (Traits::edgeValue(hostGrid->getEdge(), m) != edge[m]) return true;
+        bool changed = false;
+        if (Traits::KIND == LGD_CELL_RECORD) {
+            changed = std::memcmp(edgeRecord.data(), static_cast<const void *>(&hostGrid->getEdge()), sizeof(CELL)) != 0;
+        } else {
+            for (int m = 0; m < Traits::MEMBERS && m < 4; ++m) {
+                changed |= Traits::edgeValue(hostGrid->getEdge(), m) != edge[m];
+            }
         }
-        return false;
+        return changed;
+    }
+
+    // Rows of the host grid: cells are contiguous along x in the host grid
+    // (the reference's Grid and DisplacedGrid store the box x fastest), so a
+    // row is one pointer; the members are packed row by row through the
+    // binding's inline pack/unpack, and record cells are copied whole.
+    std::size_t rows() const
+    {
+        return (std::size_t)(DIM > 1 ? box.dimensions[1] : 1) * (DIM > 2 ? box.dimensions[2] : 1);
+    }
+
+    CELL *rowPointer(std::size_t r)
+    {
+        Coord<DIM> c = box.origin;
+        if (DIM > 1) c[1] += (int)(r % (std::size_t)box.dimensions[1]);
+        if (DIM > 2) c[2] += (int)(r / (std::size_t)box.dimensions[1]);
+        return &(*hostGrid)[c];
     }
 
     // host grid -> dense member arrays -> device (current buffer)
     void upload()
     {
         const std::size_t n = box.size();
+        const std::size_t nx = (std::size_t)box.dimensions[0];
         std::vector<char> buf;
         for (int m = 0; m < Traits::MEMBERS; ++m) {
             const std::size_t sz = Traits::memberSize(m);
             buf.resize(n * sz);
-            std::size_t i = 0;
-            for (typename CoordBox<DIM>::Iterator c = box.begin(); c != box.end(); ++c, ++i) {
-                Traits::pack(hostGrid->get(*c), m, &buf[i * sz]);
+            char *dst = buf.data();
+            for (std::size_t r = 0; r < rows(); ++r) {
+                const CELL *row = rowPointer(r);
+                if (Traits::KIND == LGD_CELL_RECORD) {
+                    std::memcpy(dst, static_cast<const void *>(row), nx * sizeof(CELL));
+                    dst += nx * sizeof(CELL);
+                } else {
+                    for (std::size_t x = 0; x < nx; ++x, dst += sz) Traits::pack(row[x], m, dst);
+                }
             }
             gb300Check(lgd_gpu_upload(handle, m, 0, buf.data(), buf.size()));
         }
@@ -467,18 +543,22 @@ private:
     {
         if (view->allValid()) return;
         const std::size_t n = box.size();
-        std::vector<std::vector<char> > bufs(Traits::MEMBERS);
+        const std::size_t nx = (std::size_t)box.dimensions[0];
+        std::vector<char> buf;
         for (int m = 0; m < Traits::MEMBERS; ++m) {
-            bufs[m].resize(n * Traits::memberSize(m));
-            gb300Check(lgd_gpu_download(handle, m, 0, bufs[m].data(), bufs[m].size()));
-        }
-        std::size_t i = 0;
-        for (typename CoordBox<DIM>::Iterator c = box.begin(); c != box.end(); ++c, ++i) {
-            CELL cell = hostGrid->get(*c);
-            for (int m = 0; m < Traits::MEMBERS; ++m) {
-                Traits::unpack(&cell, m, &bufs[m][i * Traits::memberSize(m)]);
+            const std::size_t sz = Traits::memberSize(m);
+            buf.resize(n * sz);
+            gb300Check(lgd_gpu_download(handle, m, 0, buf.data(), buf.size()));
+            const char *src = buf.data();
+            for (std::size_t r = 0; r < rows(); ++r) {
+                CELL *row = rowPointer(r);
+                if (Traits::KIND == LGD_CELL_RECORD) {
+                    std::memcpy(static_cast<void *>(row), src, nx * sizeof(CELL));
+                    src += nx * sizeof(CELL);
+                } else {
+                    for (std::size_t x = 0; x < nx; ++x, src += sz) Traits::unpack(&row[x], m, src);
+                }
             }
-            hostGrid->set(*c, cell);
         }
         view->markAllValid();
     }
@@ -506,7 +586,7 @@ private:
         if (next <= s) return;
         {
             TimeCompute t(&this->chronometer);
-            gb300Check(lgd_gpu_step(handle, 0, (int)std::min<unsigned>(next - s, 1u << 30)));
+            GB300DeviceStep<CELL>::run(handle, 0, (int)std::min<unsigned>(next - s, 1u << 30));
             gb300Check(lgd_gpu_synchronize(handle));
         }
         this->stepNum = next;

@@ -30,6 +30,8 @@ CELL_GOL_U8 = 5
 CELL_VARCOEF_F32 = 6
 CELL_VARCOEF_F64 = 7
 CELL_TEST = 8
+CELL_RECORD = 9
+RECORD_MAX_BYTES = 4096
 TEST_VON_NEUMANN = 1
 
 
@@ -110,6 +112,15 @@ def lib():
             "lgd_snapshot_info": [ctypes.c_char_p, I, P, P, P],
             "lgd_gpu_set_variant": [P, I],
             "lgd_gpu_stream": [P, P],
+            "lgd_gpu_create_records": [P, S, P, P],
+            "lgd_gpu_set_edge_record": [P, P, S],
+            "lgd_gpu_edge_record_device": [P, P],
+            "lgd_gpu_get_desc": [P, P],
+            "lgd_gpu_count_launches": [P, U64],
+            "lgd_gpu_set_fixed_point_exponent": [P, I, I],
+            "lgd_gpu_plane_bytes": [P, I, P],
+            "lgd_gpu_copy_planes": [P, I, I, I, I, P, S, I],
+            "lgd_gpu_test_bounded_waits": [P, ctypes.c_longlong, I],
             "lgd_sell_plan": [I, P, I, I, P, P, P, P, P],
             "lgd_sell_fill": [I, P, P, P, I, P, P, ctypes.c_int64, I, P, P],
             "lgd_sell_create": [I, I, ctypes.c_int64, P, P, P, P, P, I, I, P],
@@ -295,6 +306,36 @@ class Grid:
         e = ctypes.c_int()
         check(lib().lgd_gpu_fixed_point_exponent(self._h, ctypes.byref(e)))
         return e.value
+
+    def set_fixed_point_exponent(self, e: int, pin: bool = True):
+        check(lib().lgd_gpu_set_fixed_point_exponent(self._h, e, int(pin)))
+
+    def plane_bytes(self, member: int = 0) -> int:
+        n = ctypes.c_size_t()
+        check(lib().lgd_gpu_plane_bytes(self._h, member, ctypes.byref(n)))
+        return n.value
+
+    def save_planes(self, p0: int, n: int, member: int = 0, which: int = 0, out: np.ndarray | None = None):
+        """Raw planes p0 .. p0 + n - 1 of the slowest axis (device representation,
+        row padding included) into a host byte array."""
+        nbytes = n * self.plane_bytes(member)
+        if out is None:
+            out = np.empty(nbytes, dtype=np.uint8)
+        assert out.nbytes == nbytes and out.flags["C_CONTIGUOUS"]
+        check(lib().lgd_gpu_copy_planes(self._h, member, which, p0, n, _ptr(out), nbytes, 0))
+        return out
+
+    def load_planes(self, p0: int, data: np.ndarray, member: int = 0, which: int = 0):
+        a = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+        pb = self.plane_bytes(member)
+        assert a.nbytes % pb == 0
+        check(lib().lgd_gpu_copy_planes(self._h, member, which, p0, a.nbytes // pb, _ptr(a), a.nbytes, 1))
+
+    def copy_planes_device(self, p0: int, n: int, dev_ptr: int, to_grid: bool, member: int = 0, which: int = 0):
+        """Raw planes to or from device memory at dev_ptr (n * plane_bytes)."""
+        nbytes = n * self.plane_bytes(member)
+        check(lib().lgd_gpu_copy_planes(self._h, member, which, p0, n, ctypes.c_void_p(dev_ptr), nbytes,
+                                        int(to_grid)))
 
 
 # ----------------------------------------------------------- SELL-C-sigma

@@ -19,7 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblgd_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "lgd_ref")
-REFERENCE_ROOT = "/root/reference"
+# where the reference's sources lie (only in the build container)
+REFERENCE_ROOT = os.environ.get("LGD_REFERENCE_ROOT", "/root/reference")
 
 _lib = None
 

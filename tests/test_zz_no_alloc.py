@@ -36,7 +36,10 @@ def _static_sum(fn, grid, out_grid):
     """Sum of grid's current buffer via the allocation-free entry point; the
     result goes to element 0 of out_grid's device buffer."""
     d_in, pitch = grid.device_ptr(0, 0)
-    assert pitch == grid.shape[-1] * 8          # rows are dense: one flat array
+    # The library pitches rows to 128 bytes; the grids here have rows of a
+    # multiple of 16 FP64 cells (16 * 8 = 128 bytes), so their rows are dense
+    # and the buffer is one flat array of the grid's values.
+    assert pitch == grid.shape[-1] * 8
     d_out, _ = out_grid.device_ptr(0, 0)
     lgd.check(fn(d_in, grid.cells, d_out, _stream(grid)))
     grid.synchronize()
