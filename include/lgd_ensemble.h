@@ -47,11 +47,26 @@ int lgd_lbm_step_looped(lgd_lbm *h, int steps);
 int lgd_lbm_set_config(lgd_lbm *h, int tile_rows, int threads, int ctas_per_sm);
 int lgd_lbm_get_config(lgd_lbm *h, int *tile_rows, int *threads, int *ctas_per_sm);
 
-/* Pattern search over the launch shape, timing trial_steps steps per
- * candidate with CUDA events; leaves the best shape set.  The trial steps
+/* Temporal blocking: depth 1 (one step per launch, the default) or 2 (two
+ * steps per launch: each work item is a column of 32 x 8 (shape 0) or
+ * 32 x 4 (shape 1) cells of one instance marching z, the first step's
+ * populations of the column and a one-cell rim kept in shared memory;
+ * results identical to single steps), and the resident CTAs per SM of the
+ * two-step kernel (clamped to what fits).  An odd step count ends with one
+ * single step.  Plays the role of the pipeline length of the reference's
+ * CacheBlockingSimulator (parallelization/cacheblockingsimulator.h:36-56). */
+int lgd_lbm_set_time_block(lgd_lbm *h, int depth, int shape, int ctas_per_sm);
+int lgd_lbm_get_time_block(lgd_lbm *h, int *depth, int *shape, int *ctas_per_sm);
+
+/* Pattern search over the launch shape of single steps, timing trial_steps
+ * steps per candidate with CUDA events, then over the two-step kernel's
+ * tile shape and residency; leaves the fastest per step set (read it back
+ * with lgd_lbm_get_config and lgd_lbm_get_time_block).  The trial steps
  * advance the ensemble: reset or upload afterwards.  (Precedent: the
  * reference's AutoTuningSimulator with PatternOptimizer,
- * parallelization/autotuningsimulator.h:60-145, misc/patternoptimizer.h:13.) */
+ * parallelization/autotuningsimulator.h:60-145, misc/patternoptimizer.h:13,
+ * which tunes the cache-blocking simulator's pipeline length beside its
+ * wavefront, misc/cacheblockingsimulationfactory.h:26-28.) */
 int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int *ctas_per_sm, double *best_ms);
 
 /* Every instance back to equilibrium at rest. */

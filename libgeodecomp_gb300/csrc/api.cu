@@ -933,19 +933,37 @@ static void region_copy(lgd_handle *h, int member, const int *streaks, int n_str
 {
     Grid& g = grid_of(h);
     check_member(g, member, 0);
-    LGD_REQUIRE(g.desc.cell != LGD_CELL_JACOBI7_F64_FIX, LGD_ERR_UNSUPPORTED,
-                "region copies of the fixed-point grid are not supported; download the whole grid");
     const long long cells = stage_streaks(g, streaks, n_streaks);
     const int elem = g.m[member].elem;
     LGD_REQUIRE(bytes == (size_t)cells * elem, LGD_ERR_INVALID, "byte count does not match the streaks");
     if (cells == 0) return;
     LGD_REQUIRE(host != nullptr, LGD_ERR_INVALID, "null host buffer");
+    const bool fix = g.desc.cell == LGD_CELL_JACOBI7_F64_FIX;
+    if (fix && to_grid) {
+        // values the exponent cannot hold raise it first; negative ones end
+        // the sign-free fast path
+        const double *v = static_cast<const double *>(host);
+        double m = 0.0;
+        bool neg = false;
+        for (long long i = 0; i < cells; ++i) {
+            LGD_REQUIRE(std::isfinite(v[i]), LGD_ERR_INVALID, "grid holds a non-finite value");
+            m = std::fmax(m, std::fabs(v[i]));
+            neg |= v[i] < 0.0;
+        }
+        if (neg) g.fix_nonneg = false;
+        if (exp_bound(m) > g.fix_exp) raise_fix_exp(g, exp_bound(m));
+    }
     void *d = nullptr;
     LGD_CHECK_CUDA(cudaMallocAsync(&d, bytes, g.stream));
     if (to_grid) {
         LGD_CHECK_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, g.stream));
     }
-    launch_streak_copy(g, member, 0, g.d_streaks, g.d_streak_prefix, n_streaks, cells, d, to_grid);
+    if (fix) {
+        // FP64 values at the boundary, fixed point on the device
+        launch_streak_copy_fix(g, g.d_streaks, g.d_streak_prefix, n_streaks, cells, (double *)d, to_grid);
+    } else {
+        launch_streak_copy(g, member, 0, g.d_streaks, g.d_streak_prefix, n_streaks, cells, d, to_grid);
+    }
     if (!to_grid) {
         LGD_CHECK_CUDA(cudaMemcpyAsync(host, d, bytes, cudaMemcpyDeviceToHost, g.stream));
     }

@@ -304,6 +304,36 @@ __global__ void streak_copy_records_kernel(unsigned char *base, long pitch_bytes
     }
 }
 
+// streaks of a fixed-point grid as FP64 values (k * 2^(scale_exp - 57))
+__global__ void streak_copy_fix_kernel(View<long long> v, const int *streaks, const long long *prefix, int n_streaks,
+                                       long long cells, double *packed, bool to_grid, int scale_exp)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= cells) return;
+    int x, y, z;
+    locate_cell(streaks, prefix, n_streaks, i, &x, &y, &z);
+    if (to_grid) {
+        v.at(x, y, z) = __double2ll_rn(ldexp(packed[i], LGD_FIX_BITS - scale_exp));
+    } else {
+        packed[i] = ldexp((double)v.at(x, y, z), scale_exp - LGD_FIX_BITS);
+    }
+}
+
+int fix_scale_exp(const Grid& g);
+
+void launch_streak_copy_fix(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells,
+                            double *d_packed, bool to_grid)
+{
+    if (cells == 0) return;
+    const int threads = 256;
+    const long long blocks = (cells + threads - 1) / threads;
+    streak_copy_fix_kernel<<<(unsigned)blocks, threads, 0, g.stream>>>(view_of<long long>(g, 0, 0), d_streaks,
+                                                                      d_prefix, n_streaks, cells, d_packed, to_grid,
+                                                                      fix_scale_exp(g));
+    check_launch("fixed-point streak copy");
+    ++g.launches;
+}
+
 template<typename T>
 __global__ void streak_copy_kernel(View<T> v, const int *streaks, const long long *prefix, int n_streaks,
                                    long long cells, T *packed, bool to_grid)

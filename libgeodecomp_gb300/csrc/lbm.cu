@@ -25,6 +25,7 @@
 // pattern search (lgd_lbm_tune), the method of the reference's
 // PatternOptimizer (misc/patternoptimizer.h:13) applied to this kernel.
 #include <algorithm>
+#include <mutex>
 #include <cstring>
 #include <vector>
 
@@ -64,6 +65,15 @@ struct Lbm {
     bool idx32;         // every instance indexable with 32 bits (19 L^3 < 2^31)
     int variant;        // 0: plain loads and stores; 1: read-only-path loads, evict-first stores
     uint64_t launches;
+    // temporal blocking: depth 1 (one step per launch) or 2 (lbm_tb2_kernel),
+    // tile shape 0 (32 x 8) or 1 (32 x 4), resident CTAs per SM of the
+    // depth-2 kernel; its work items are (instance, x0, y0) columns
+    int depth;
+    int tb_shape;
+    int tb_ctas;
+    int4 *d_cols;
+    int n_cols;
+    int cols_shape;
 };
 
 // D3Q19 directions in the reference's naming order: C, N, E, W, S, T, B,
@@ -171,9 +181,10 @@ struct PullAll<R, 19, IDX, NC, INTERIOR> {
     static __device__ __forceinline__ void run(const R *, IDX, IDX, int, int, int, int, R, R *) {}
 };
 
-// BGK collision, operation order of the oracle's lgd_d3q19_collide
-template<typename R, typename IDX, int NC>
-__device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict__ dst, IDX n3, IDX cell)
+// BGK collision, operation order of the oracle's lgd_d3q19_collide; put(i,
+// v) stores post-collision population i
+template<typename R, typename PUT>
+__device__ __forceinline__ void collide_to(const R *f, R omega, PUT put)
 {
     typedef LbmArith<R> A;
     R rho = f[0];
@@ -193,15 +204,20 @@ __device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict
     const R keep = A::sub((R)1.0, omega);
     const R w1 = A::mul(omega, (R)(1.0 / 6.0));
     const R w2 = A::mul(omega, (R)(1.0 / 12.0));
-    Mem<NC>::st(dst + cell, A::add(A::mul(keep, f[0]), A::mul(omega, d)));
+    put(0, A::add(A::mul(keep, f[0]), A::mul(omega, d)));
 #pragma unroll
     for (int i = 1; i < 19; ++i) {
         // eu = ex * ux + ey * uy + ez * uz, evaluated as the oracle does
         const R eu = A::add(A::add(A::mul((R)c_ex[i], ux), A::mul((R)c_ey[i], uy)), A::mul((R)c_ez[i], uz));
         const R wi = (i < 7) ? w1 : w2;
-        Mem<NC>::st(dst + (i * n3 + cell),
-                    A::add(A::mul(keep, f[i]), A::mul(wi, A::add(A::add(d, eu), A::mul((R)1.5, A::mul(eu, eu))))));
+        put(i, A::add(A::mul(keep, f[i]), A::mul(wi, A::add(A::add(d, eu), A::mul((R)1.5, A::mul(eu, eu))))));
     }
+}
+
+template<typename R, typename IDX, int NC>
+__device__ __forceinline__ void collide_store(const R *f, R omega, R *__restrict__ dst, IDX n3, IDX cell)
+{
+    collide_to<R>(f, omega, [&](int i, R v) { Mem<NC>::st(dst + ((IDX)i * n3 + cell), v); });
 }
 
 // Cells of rows [y0, y1) of plane z (contiguous in memory), the threads
@@ -281,6 +297,125 @@ __global__ void lbm_single_kernel(const LbmInstance *__restrict__ inst, int j, c
     const int y0 = blockIdx.x * rows_per_block;
     if (y0 >= in.L) return;
     lbm_item<R, IDX, NC>(in, A, B, z, y0, min(in.L, y0 + rows_per_block), threadIdx.x, blockDim.x);
+}
+
+// ------------------------------------------------ two steps per launch
+// Temporal blocking of depth 2.  A work item is a column of one instance:
+// TX x TY cells of every z plane.  The CTA marches z; at each plane it
+// first computes step 1 for the tile plus a one-cell rim (the cells whose
+// populations step 2 pulls), pulling from the input grid and keeping the 19
+// post-collision populations in a ring of three planes in shared memory,
+// then step 2 for the tile at the plane below, pulling from the ring and
+// writing the output grid.  Walls bounce back from the cell itself at
+// either level, exactly as the single step does, so the result is the two
+// single steps' bit for bit; HBM traffic per two steps is one read of the
+// input (plus the rim's, about a third more, partly from L2) and one write.
+template<int TX, int TY>
+struct Tb2Geo {
+    static constexpr int THREADS = TX * TY;
+    static constexpr int HX = TX + 2;
+    static constexpr int HY = TY + 2;
+    static constexpr int HC = HX * HY;          // step-1 cells of one plane
+    template<typename R>
+    static constexpr size_t smem() { return (size_t)3 * 19 * HC * sizeof(R); }
+};
+
+// step-2 population I of tile cell (tx, ty) at plane zz from the ring
+template<typename R, int I, int TX, int TY>
+__device__ __forceinline__ R tb2_pull(const R *__restrict__ ring, int L, int x, int y, int zz, int tx, int ty, R lid)
+{
+    typedef Tb2Geo<TX, TY> G;
+    const int sx = x - Q<I>::ex;
+    const int sy = y - Q<I>::ey;
+    const int sz = zz - Q<I>::ez;
+    if ((unsigned)sx < (unsigned)L && (unsigned)sy < (unsigned)L && (unsigned)sz < (unsigned)L) {
+        return ring[((sz % 3) * 19 + I) * G::HC + (ty + 1 - Q<I>::ey) * G::HX + (tx + 1 - Q<I>::ex)];
+    }
+    R v = ring[((zz % 3) * 19 + Q<I>::opp) * G::HC + (ty + 1) * G::HX + (tx + 1)];
+    if (Q<I>::ey == -1 && Q<I>::ex != 0 && y == L - 1) {
+        const R w = (I < 7) ? (R)(1.0 / 18.0) : (R)(1.0 / 36.0);
+        v = LbmArith<R>::add(v, LbmArith<R>::mul(LbmArith<R>::mul((R)6.0, w), (R)Q<I>::ex * lid));
+    }
+    return v;
+}
+
+template<typename R, int I, int TX, int TY>
+struct Tb2PullAll {
+    static __device__ __forceinline__ void run(const R *ring, int L, int x, int y, int zz, int tx, int ty, R lid, R *f)
+    {
+        f[I] = tb2_pull<R, I, TX, TY>(ring, L, x, y, zz, tx, ty, lid);
+        Tb2PullAll<R, I + 1, TX, TY>::run(ring, L, x, y, zz, tx, ty, lid, f);
+    }
+};
+
+template<typename R, int TX, int TY>
+struct Tb2PullAll<R, 19, TX, TY> {
+    static __device__ __forceinline__ void run(const R *, int, int, int, int, int, int, R, R *) {}
+};
+
+template<typename R, typename IDX, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+lbm_tb2_kernel(const LbmInstance *__restrict__ inst, const int4 *__restrict__ items, int n_items, int *counter,
+               const R *__restrict__ A, R *__restrict__ B)
+{
+    typedef Tb2Geo<TX, TY> G;
+    extern __shared__ __align__(16) unsigned char tb2_smem[];
+    R *ring = reinterpret_cast<R *>(tb2_smem);
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items) break;
+        const int4 w = items[it];
+        const LbmInstance in = inst[w.x];
+        const int L = in.L;
+        const int x0 = w.y;
+        const int y0 = w.z;
+        const IDX n3 = ((IDX)L * L * L + 31) & ~(IDX)31;
+        const R *src = A + in.base;
+        R *dst = B + in.base;
+        const R omega = (sizeof(R) == 8) ? (R)in.omega : (R)in.omega_f;
+        const R lid = (sizeof(R) == 8) ? (R)in.lid : (R)in.lid_f;
+        for (int z = 0; z <= L; ++z) {
+            if (z < L) {
+                // step 1 at plane z: the tile and its rim, inside the instance
+                R *plane = ring + (z % 3) * 19 * G::HC;
+                for (int c = tid; c < G::HC; c += G::THREADS) {
+                    const int x = x0 - 1 + c % G::HX;
+                    const int y = y0 - 1 + c / G::HX;
+                    if ((unsigned)x < (unsigned)L && (unsigned)y < (unsigned)L) {
+                        const IDX cell = ((IDX)z * L + y) * L + x;
+                        R f[19];
+                        if ((unsigned)(x - 1) < (unsigned)(L - 2) && (unsigned)(y - 1) < (unsigned)(L - 2) &&
+                            (unsigned)(z - 1) < (unsigned)(L - 2)) {
+                            PullAll<R, 0, IDX, 0, true>::run(src, n3, cell, L, x, y, z, lid, f);
+                        } else {
+                            PullAll<R, 0, IDX, 0, false>::run(src, n3, cell, L, x, y, z, lid, f);
+                        }
+                        collide_to<R>(f, omega, [&](int i, R v) { plane[i * G::HC + c] = v; });
+                    }
+                }
+            }
+            __syncthreads();
+            if (z >= 1) {
+                // step 2 at plane z - 1: the tile, from the ring
+                const int zz = z - 1;
+                const int tx = tid % TX;
+                const int ty = tid / TX;
+                const int x = x0 + tx;
+                const int y = y0 + ty;
+                if (x < L && y < L) {
+                    R f[19];
+                    Tb2PullAll<R, 0, TX, TY>::run(ring, L, x, y, zz, tx, ty, lid, f);
+                    const IDX cell = ((IDX)zz * L + y) * L + x;
+                    collide_store<R, IDX, 0>(f, omega, dst, n3, cell);
+                }
+            }
+            __syncthreads();        // the slot of plane z - 2 is written at z + 1
+        }
+    }
 }
 
 template<typename R>
@@ -377,6 +512,91 @@ static void launch_step(Lbm& e, int which_counter, int src)
     LGD_CHECK_CUDA(cudaLaunchKernel(persistent_fn(e), dim3(grid), dim3(e.threads), args, 0, e.stream));
 }
 
+template<typename R, typename IDX, int TX, int TY>
+static const void *tb2_fn()
+{
+    return (const void *)lbm_tb2_kernel<R, IDX, TX, TY>;
+}
+
+template<typename R, int TX, int TY>
+static const void *tb2_fn_idx(const Lbm& e)
+{
+    return e.idx32 ? tb2_fn<R, int, TX, TY>() : tb2_fn<R, long long, TX, TY>();
+}
+
+// the depth-2 kernel of the ensemble's precision, index width and shape,
+// its threads per CTA and shared memory per CTA
+static const void *tb2_kernel(const Lbm& e, int shape, int *threads, size_t *smem)
+{
+    if (shape == 1) {
+        *threads = Tb2Geo<32, 4>::THREADS;
+        *smem = e.precision == 4 ? Tb2Geo<32, 4>::smem<float>() : Tb2Geo<32, 4>::smem<double>();
+        return e.precision == 4 ? tb2_fn_idx<float, 32, 4>(e) : tb2_fn_idx<double, 32, 4>(e);
+    }
+    *threads = Tb2Geo<32, 8>::THREADS;
+    *smem = e.precision == 4 ? Tb2Geo<32, 8>::smem<float>() : Tb2Geo<32, 8>::smem<double>();
+    return e.precision == 4 ? tb2_fn_idx<float, 32, 8>(e) : tb2_fn_idx<double, 32, 8>(e);
+}
+
+// column work items of a depth-2 tile shape, largest instances first
+static void build_cols(Lbm& e, int shape)
+{
+    const int TX = 32, TY = shape == 1 ? 4 : 8;
+    std::vector<int> order(e.count);
+    for (int j = 0; j < e.count; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e.inst[a].L > e.inst[b].L; });
+    std::vector<int4> cols;
+    for (int j : order) {
+        const int L = e.inst[j].L;
+        for (int y0 = 0; y0 < L; y0 += TY) {
+            for (int x0 = 0; x0 < L; x0 += TX) cols.push_back(make_int4(j, x0, y0, 0));
+        }
+    }
+    if (e.d_cols) cudaFree(e.d_cols);
+    e.d_cols = nullptr;
+    LGD_CHECK_CUDA(cudaMalloc(&e.d_cols, sizeof(int4) * cols.size()));
+    LGD_CHECK_CUDA(cudaMemcpyAsync(e.d_cols, cols.data(), sizeof(int4) * cols.size(), cudaMemcpyHostToDevice, e.stream));
+    LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
+    e.n_cols = (int)cols.size();
+    e.cols_shape = shape;
+}
+
+// resident CTAs per SM of a depth-2 kernel, set up once per device and kernel
+static int tb2_resident(const void *fn, int threads, size_t smem)
+{
+    static std::mutex m;
+    static std::vector<std::pair<std::pair<int, const void *>, int> > known;
+    int dev = 0;
+    LGD_CHECK_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(m);
+    for (const auto& k : known) {
+        if (k.first.first == dev && k.first.second == fn) return k.second;
+    }
+    LGD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    known.push_back(std::make_pair(std::make_pair(dev, fn), per_sm));
+    return per_sm;
+}
+
+// two steps of every instance in one launch (src -> 1 - src)
+static void launch_tb2(Lbm& e, int src)
+{
+    int threads = 0;
+    size_t smem = 0;
+    const void *fn = tb2_kernel(e, e.tb_shape, &threads, &smem);
+    const int per_sm = tb2_resident(fn, threads, smem);
+    LGD_REQUIRE(per_sm >= 1, LGD_ERR_UNSUPPORTED, "the two-step kernel does not fit on this GPU");
+    if (e.cols_shape != e.tb_shape || e.d_cols == nullptr) build_cols(e, e.tb_shape);
+    LGD_CHECK_CUDA(cudaMemsetAsync(e.d_counter + 2, 0, sizeof(int), e.stream));
+    const int grid = e.sms * std::min(std::max(1, e.tb_ctas), per_sm);
+    int *counter = e.d_counter + 2;
+    const void *a = e.buf[src];
+    void *b = e.buf[1 - src];
+    void *args[] = {&e.d_inst, &e.d_cols, &e.n_cols, &counter, &a, &b};
+    LGD_CHECK_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, e.stream));
+}
+
 static void launch_single(Lbm& e, int j, dim3 grid)
 {
     if (e.variant == 1) {
@@ -429,6 +649,20 @@ static void set_config(Lbm& e, int ty, int threads, int ctas)
 
 static void run_steps(Lbm& e, int steps)
 {
+    if (e.depth == 2) {
+        // pairs of steps in one launch each, a last odd step on its own
+        for (; steps >= 2; steps -= 2) {
+            launch_tb2(e, e.cur);
+            ++e.launches;
+            e.cur = 1 - e.cur;
+        }
+        if (steps == 1) {
+            launch_step(e, 0, e.cur);
+            ++e.launches;
+            e.cur = 1 - e.cur;
+        }
+        return;
+    }
     int s = 0;
     if (e.cur == 1 && steps > 0) {
         launch_step(e, 0, 1);
@@ -455,6 +689,7 @@ static void lbm_free(Lbm& e)
     cudaFree(e.buf[1]);
     cudaFree(e.d_inst);
     cudaFree(e.d_items);
+    cudaFree(e.d_cols);
     cudaFree(e.d_counter);
     if (e.stream) cudaStreamDestroy(e.stream);
 }
@@ -506,7 +741,9 @@ int lgd_lbm_create(int count, const int32_t *edges, const double *omegas, double
             LGD_CHECK_CUDA(cudaMalloc(&e->d_inst, sizeof(LbmInstance) * count));
             LGD_CHECK_CUDA(cudaMemcpyAsync(e->d_inst, e->inst.data(), sizeof(LbmInstance) * count,
                                            cudaMemcpyHostToDevice, e->stream));
-            LGD_CHECK_CUDA(cudaMalloc(&e->d_counter, sizeof(int) * 2));
+            LGD_CHECK_CUDA(cudaMalloc(&e->d_counter, sizeof(int) * 3));   // two captured steps, the depth-2 launch
+            e->depth = 1;
+            e->tb_ctas = 1;
             dim3 grid(256, count);
             if (precision == 4) {
                 lbm_rest_kernel<float><<<grid, 256, 0, e->stream>>>(e->d_inst, count, (float *)e->buf[0]);
@@ -628,6 +865,42 @@ int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int 
             c = bc;
         }
         set_config(e, tys[a], ths[b], cts[c]);
+        // then temporal blocking: two steps per launch in each tile shape
+        // and residency; the fastest per step wins, one step per launch
+        // included (the reference's autotuner tunes the pipeline length of
+        // its cache-blocking simulator the same way,
+        // misc/cacheblockingsimulationfactory.h:26-28)
+        e.depth = 1;
+        int best_depth = 1, best_shape = 0, best_ctas = 1;
+        for (int shape = 0; shape < 2; ++shape) {
+            int threads = 0;
+            size_t smem = 0;
+            const void *fn = tb2_kernel(e, shape, &threads, &smem);
+            const int per_sm = tb2_resident(fn, threads, smem);
+            for (int ct = 1; ct <= std::min(per_sm, 4); ++ct) {
+                e.depth = 2;
+                e.tb_shape = shape;
+                e.tb_ctas = ct;
+                run_steps(e, 2);   // warm (builds the columns)
+                const int n = 2 * ((trial_steps + 1) / 2);
+                LGD_CHECK_CUDA(cudaEventRecord(t0, e.stream));
+                run_steps(e, n);
+                LGD_CHECK_CUDA(cudaEventRecord(t1, e.stream));
+                LGD_CHECK_CUDA(cudaEventSynchronize(t1));
+                float ms = 0.f;
+                LGD_CHECK_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+                const double t = ms / n;
+                if (t < best * 0.99) {
+                    best = t;
+                    best_depth = 2;
+                    best_shape = shape;
+                    best_ctas = ct;
+                }
+            }
+        }
+        e.depth = best_depth;
+        e.tb_shape = best_shape;
+        e.tb_ctas = best_ctas;
         LGD_CHECK_CUDA(cudaStreamSynchronize(e.stream));
         cudaEventDestroy(t0);
         cudaEventDestroy(t1);
@@ -635,6 +908,36 @@ int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int 
         if (threads) *threads = e.threads;
         if (ctas_per_sm) *ctas_per_sm = e.ctas_per_sm;
         if (best_ms) *best_ms = best;
+    });
+}
+
+int lgd_lbm_set_time_block(lgd_lbm *h, int depth, int shape, int ctas_per_sm)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        LGD_REQUIRE(depth == 1 || depth == 2, LGD_ERR_INVALID, "the ensemble fuses one or two steps per launch");
+        LGD_REQUIRE(shape == 0 || shape == 1, LGD_ERR_INVALID, "tile shape must be 0 (32 x 8) or 1 (32 x 4)");
+        LGD_REQUIRE(ctas_per_sm >= 1 && ctas_per_sm <= 32, LGD_ERR_INVALID, "CTAs per SM out of range");
+        if (depth == 2) {
+            int threads = 0;
+            size_t smem = 0;
+            const void *fn = tb2_kernel(e, shape, &threads, &smem);
+            LGD_REQUIRE(tb2_resident(fn, threads, smem) >= 1, LGD_ERR_UNSUPPORTED,
+                        "the two-step kernel does not fit on this GPU");
+        }
+        e.depth = depth;
+        e.tb_shape = shape;
+        e.tb_ctas = ctas_per_sm;
+    });
+}
+
+int lgd_lbm_get_time_block(lgd_lbm *h, int *depth, int *shape, int *ctas_per_sm)
+{
+    return guard([&] {
+        Lbm& e = lbm_of(h);
+        if (depth) *depth = e.depth;
+        if (shape) *shape = e.tb_shape;
+        if (ctas_per_sm) *ctas_per_sm = e.tb_ctas;
     });
 }
 

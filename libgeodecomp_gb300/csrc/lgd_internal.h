@@ -207,6 +207,9 @@ void launch_fill(Grid& g, int member, int which, uint64_t seed, int stream, int 
 void launch_checksum(Grid& g, int member, int which, double *out);
 void launch_streak_copy(Grid& g, int member, int which, const int *d_streaks, const long long *d_prefix,
                         int n_streaks, long long cells, void *d_packed, bool to_grid);
+// the same for a fixed-point grid's current buffer, FP64 values at the boundary
+void launch_streak_copy_fix(Grid& g, const int *d_streaks, const long long *d_prefix, int n_streaks, long long cells,
+                            double *d_packed, bool to_grid);
 
 // SplitMix64 key derivation shared with the fill kernel
 uint64_t stream_key(uint64_t seed, int stream);

@@ -151,6 +151,8 @@ def lib():
             "lgd_lbm_stream": [P, P],
             "lgd_lbm_launch_count": [P, P],
             "lgd_lbm_set_variant": [P, I],
+            "lgd_lbm_set_time_block": [P, I, I, I],
+            "lgd_lbm_get_time_block": [P, P, P, P],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -573,3 +575,12 @@ class LbmEnsemble:
     def set_variant(self, variant: int):
         """Memory path (identical results): 0 plain, 1 read-only loads + evict-first stores."""
         check(lib().lgd_lbm_set_variant(self._h, variant))
+
+    def set_time_block(self, depth: int, shape: int = 0, ctas_per_sm: int = 1):
+        """Steps per launch (1 or 2), the two-step kernel's tile shape and residency."""
+        check(lib().lgd_lbm_set_time_block(self._h, depth, shape, ctas_per_sm))
+
+    def time_block(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().lgd_lbm_get_time_block(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value

@@ -117,3 +117,54 @@ def test_lbm_upload_roundtrip_and_errors():
         assert err.value.code == lgd.ERR_RANGE
     with pytest.raises(lgd.LGDError):
         lgd.LbmEnsemble([4], [2.5])
+
+
+# ----------------------------------------------- two steps per launch
+@pytest.mark.parametrize("shape,ctas", [(0, 1), (0, 2), (1, 1), (1, 3)])
+@pytest.mark.parametrize("steps", [10, 11])
+def test_lbm_two_steps_per_launch_bit_identical_fp64(shape, ctas, steps):
+    """Depth 2 (the first step's populations of a column and its rim in
+    shared memory) equals single steps and the oracle bit for bit: uneven
+    instances smaller and larger than a tile, edges that are not multiples
+    of the tile, an odd step count ending with one single step."""
+    edges = [5, 12, 2, 33, 17, 3, 40]
+    omegas = [1.0, 1.3, 1.9, 0.7, 1.55, 1.2, 1.8]
+    with lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=8) as e:
+        e.set_time_block(2, shape, ctas)
+        before = e.launch_count()
+        e.step(steps)
+        assert e.launch_count() - before == steps // 2 + steps % 2
+        assert e.time_block() == (2, shape, ctas)
+        for j, (L, om) in enumerate(zip(edges, omegas)):
+            np.testing.assert_array_equal(e.download(j), oracle.lbm(L, steps, om, 0.05), err_msg=str(j))
+
+
+def test_lbm_two_steps_fp32_equal_single_steps_and_reference_L24():
+    edges, omegas = workloads.lbm_ensemble(20, seed=5, edge_min=6, edge_max=70)
+    with lgd.LbmEnsemble(edges, omegas, precision=4) as a, lgd.LbmEnsemble(edges, omegas, precision=4) as b:
+        a.set_time_block(2, 0, 2)
+        a.step(8)
+        b.step(8)
+        for j in range(len(edges)):
+            np.testing.assert_array_equal(a.download(j), b.download(j))
+    g = load("lbm_L24")
+    with lgd.LbmEnsemble([int(g["L"])], [float(g["omega"])], lid=float(g["lid"]), precision=8) as e:
+        e.set_time_block(2, 1, 1)
+        e.step(int(g["steps"]))
+        assert sha(e.download(0)) == str(g["sha256"])
+
+
+def test_lbm_tuner_reports_depth_and_results_stay_exact():
+    edges, omegas = workloads.lbm_ensemble(24, seed=6, edge_min=16, edge_max=48)
+    with lgd.LbmEnsemble(edges, omegas, precision=8) as e:
+        e.tune(trial_steps=2)
+        depth, shape, ctas = e.time_block()
+        assert depth in (1, 2) and shape in (0, 1) and ctas >= 1
+        e.reset()
+        e.step(7)
+        np.testing.assert_array_equal(e.download(5), oracle.lbm(int(edges[5]), 7, float(omegas[5]), 0.05))
+    with lgd.LbmEnsemble([6], [1.2], precision=8) as e:
+        with pytest.raises(lgd.LGDError):
+            e.set_time_block(3, 0, 1)
+        with pytest.raises(lgd.LGDError):
+            e.set_time_block(2, 2, 1)

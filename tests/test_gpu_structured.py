@@ -214,10 +214,16 @@ def test_upload_rejects_wrong_size():
         assert e.value.code == lgd.ERR_INVALID
 
 
-def test_region_save_load_roundtrip():
+@pytest.mark.parametrize("cell", [lgd.CELL_JACOBI7_F64, lgd.CELL_JACOBI7_F64_FIX])
+def test_region_save_load_roundtrip(cell):
+    """Streak copies (the drop-in's writers read planes this way); the
+    fixed-point grid converts at the boundary, exactly for values whose
+    53-bit mantissa fits its 57 fraction bits.  Loading negative values
+    into the fixed-point grid ends its sign-free fast path and the next
+    steps stay right."""
     u0 = workloads.jacobi_initial(30, 20, 10, seed=4)
     streaks = [(3, 2, 1, 17), (0, 19, 9, 30), (5, 5, 5, 6)]
-    with lgd.Grid(lgd.CELL_JACOBI7_F64, u0.shape) as g:
+    with lgd.Grid(cell, u0.shape) as g:
         g.upload(0, u0)
         got = g.save_region(0, streaks)
         exp = np.concatenate([u0[z, y, x:e] for (x, y, z, e) in streaks])
@@ -228,6 +234,15 @@ def test_region_save_load_roundtrip():
     for (x, y, z, e) in streaks:
         ref[z, y, x:e] = -ref[z, y, x:e]
     np.testing.assert_array_equal(u1, ref)
+    if cell == lgd.CELL_JACOBI7_F64_FIX:
+        with lgd.Grid(cell, u0.shape) as g:
+            g.upload(0, u0)
+            g.load_region(0, streaks, -got)
+            g.step(4)
+            out = g.download(0)
+        # four steps of values in (-1, 1): the fixed-point rounding (4 x
+        # 2^-58) and the reference's own (seven roundings per step)
+        assert np.max(np.abs(out - oracle.jacobi7(ref, 4))) < 1e-14
 
 
 def test_checksum_matches_host_sum():
