@@ -902,12 +902,18 @@ def run_surrogate(args):
     u0 = torch.tensor(u0_np, dtype=torch.float32, device="cuda").contiguous()
     kap = torch.tensor(k_np, dtype=torch.float32, device="cuda").contiguous()
     # FP64 reference with the FP64 stencil (bit-identical to the reference's
-    # simulator at small sizes, see tests)
+    # simulator at small sizes, see tests), timed: the comparator an FP64
+    # user would otherwise run
     ref = S.PlainStencil(n, precision=8)
     try:
         u64 = torch.tensor(u0_np, dtype=torch.float64, device="cuda").contiguous()
         ref.set_kappa(torch.tensor(k_np, dtype=torch.float64, device="cuda").contiguous())
+        ref.run(u64.clone(), 16)                     # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         ref.run(u64, steps)
+        torch.cuda.synchronize()
+        t_fp64 = time.perf_counter() - t0
     finally:
         ref.close()
     S.run_plain(u0, kap, 16)                         # warm-up
@@ -926,7 +932,10 @@ def run_surrogate(args):
                    "kappa": "GRF length 16 mapped to [0.02, 0.15]", "net": "4 x conv3^3, 24 ch, GELU, residual",
                    "steps_per_call": S.STEPS_PER_CALL, "judge_every_calls": S.CALLS_PER_JUDGE,
                    "judge_tol": args.judge_tol, "trajectories": args.trajectories, "train_iters": args.train_iters},
-        "plain_fp32_s": round(t_plain, 4), "surrogate_judge_s": round(t_sur, 4),
+        "plain_fp32_s": round(t_plain, 4), "plain_fp64_s": round(t_fp64, 4), "surrogate_judge_s": round(t_sur, 4),
+        "comparators": {"fp64_over_surrogate": round(t_fp64 / t_sur, 4),
+                        "fp64_over_relaxed_surrogate": round(t_fp64 / t_rel, 4),
+                        "fp32_over_surrogate": round(t_plain / t_sur, 4)},
         "rel_l2_vs_fp64": {"plain_fp32": S.rel_l2(u_plain, u64), "surrogate_judge": S.rel_l2(u_sur, u64)},
         "judge": {"segments": stats["segments"], "fallbacks": stats["fallbacks"],
                   "max_error": max(stats["judge_errors"]) if stats["judge_errors"] else None},

@@ -25,6 +25,7 @@
 // pattern search (lgd_lbm_tune), the method of the reference's
 // PatternOptimizer (misc/patternoptimizer.h:13) applied to this kernel.
 #include <algorithm>
+#include <limits>
 #include <mutex>
 #include <cstring>
 #include <vector>
@@ -823,6 +824,9 @@ int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int 
         LGD_CHECK_CUDA(cudaEventCreate(&t1));
         // the trial runs advance the ensemble: callers reset or upload afterwards
         auto measure = [&](int ty, int th, int ct) -> double {
+            int fits = 0;
+            LGD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fits, persistent_fn(e), th, 0));
+            if (fits < 1) return std::numeric_limits<double>::infinity();   // too many registers for th threads
             set_config(e, ty, th, ct);
             run_steps(e, 2);   // warm
             LGD_CHECK_CUDA(cudaEventRecord(t0, e.stream));
