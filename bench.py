@@ -63,7 +63,7 @@ import numpy as np  # noqa: E402
 
 JACOBI_METRIC = "Jacobi3D GLUPS & HBM GB/s vs 8 TB/s"
 METRICS = {"gol_u8_8192": "Game of Life GLUPS", "sell_f64_4m": "SELL-C-sigma diffusion GB/s and s/step",
-           "lbm_d3q19_ensemble_512": "D3Q19 ensemble GLUPS (one persistent launch per step)",
+           "lbm_d3q19_ensemble_512": "D3Q19 ensemble GLUPS (persistent launches, autotuned steps per launch)",
            "varcoef_f32_256": "variable-coefficient diffusion GLUPS"}
 DTYPES = {"gol_u8_8192": "u8", "lbm_d3q19_ensemble_512": "f32", "varcoef_f32_256": "f32", "jacobi7_f32_512": "f32",
           "sell_f64_4m": "f64", "jacobi7_f64_ieee_512": "f64",
@@ -425,12 +425,13 @@ class VarcoefWorkload:
 
 class LbmWorkload:
     """512 D3Q19 lid-driven cavities, edges uniform in {32..192}, omega
-    uniform in [1.0, 1.9), lid 0.05, FP32; one persistent launch per step,
-    launch shape from the library's pattern-search tuner."""
+    uniform in [1.0, 1.9), lid 0.05, FP32; one persistent launch per step or
+    one two-step launch per pair of steps, launch shape and steps per launch
+    from the library's pattern-search tuner."""
     run_steps = 500
     bytes_per_unit = 152     # 19 FP32 reads + 19 FP32 writes per cell
 
-    def __init__(self, instances=512, edge_max=192, tune=True):
+    def __init__(self, instances=512, edge_max=192, tune=True, time_block=None):
         from libgeodecomp_gb300 import lgd, workloads
         self.lgd = lgd
         self.name = "lbm_d3q19_ensemble_512"
@@ -447,11 +448,17 @@ class LbmWorkload:
             self.e.reset()
         else:
             ty, th, ct = self.e.config()
+        if time_block:
+            self.e.set_time_block(*time_block)
+        depth, shape, ctas = self.e.time_block()
+        self.depth = depth
         self.setup = {"cells": self.units, "work_items": self.items, "tune_s": round(time.perf_counter() - t0, 2),
-                      "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct}}
+                      "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct},
+                      "tuned_time_block": {"steps_per_launch": depth, "tile": "32x8" if shape == 0 else "32x4",
+                                           "ctas_per_sm": ctas}}
 
     def traffic_key(self):
-        return self.name
+        return self.name + ("_tb2" if self.depth == 2 else "")
 
     def stream(self):
         return self.e.stream()
@@ -481,7 +488,9 @@ class LbmWorkload:
 
 def make_workload(name, args):
     if name == "lbm_d3q19_ensemble_512":
-        return LbmWorkload(instances=args.lbm_instances, edge_max=args.lbm_edge_max, tune=not args.lbm_no_tune)
+        tb = tuple(int(v) for v in args.lbm_time_block.split(",")) if args.lbm_time_block else None
+        return LbmWorkload(instances=args.lbm_instances, edge_max=args.lbm_edge_max, tune=not args.lbm_no_tune,
+                           time_block=tb)
     if name == "jacobi7_f64_512":
         return JacobiWorkload(ieee=False, edge=args.size)
     if name == "jacobi7_f64_ieee_512":
@@ -991,6 +1000,8 @@ def main():
     ap.add_argument("--lbm-instances", type=int, default=512, help="ensemble size (smaller for profiling captures)")
     ap.add_argument("--lbm-edge-max", type=int, default=192)
     ap.add_argument("--lbm-no-tune", action="store_true", help="keep the default launch shape (profiling captures)")
+    ap.add_argument("--lbm-time-block", default="", help="depth,shape,ctas: steps per launch of the ensemble, "
+                    "overriding the tuner (profiling captures)")
     ap.add_argument("--surrogate", action="store_true", help="run the learned-surrogate time-to-solution benchmark")
     ap.add_argument("--surrogate-size", type=int, default=256)
     ap.add_argument("--surrogate-steps", type=int, default=4096)
