@@ -11,14 +11,15 @@ HBM.
 
   value     GLUPS with the grid resident in HBM, timed with CUDA events on
             the library's stream over exactly --steps time steps.
-  roofline  per launch (one pass): achieved = the pass's algorithmic bytes
-            (every cell read once and written once) / the launch's average
-            time, frac = achieved / the measured HBM copy bandwidth,
-            traffic = DRAM bytes per launch from the committed ncu
-            summaries; where a pass advances several steps,
-            effective_gbs_one_step_per_pass and frac_one_step_per_pass
-            count the algorithmic bytes of every step instead (the
-            bandwidth a one-step-per-pass code would need for this GLUPS).
+  roofline  per launch: achieved = the launch's algorithmic bytes (16 B
+            per lattice-site update for FP64 Jacobi: one read and one write
+            of every cell and time step, times the updates the launch
+            performs) / the launch's average time, frac = achieved / the
+            measured HBM copy bandwidth, traffic = DRAM bytes per launch
+            from the committed ncu summaries.  Where a launch fuses several
+            steps (temporal blocking) achieved can exceed the copy
+            bandwidth; per_pass_gbs and frac_per_pass count one read and
+            one write per cell and launch, which is what HBM sees.
   e2e       the same metric through the C ABI with host buffers: upload
             from pinned host memory, the configuration's run length of time
             steps, download of the result - per e2e step.
@@ -553,25 +554,29 @@ def time_steps(torch, w, steps):
 
 
 def roofline_of(w, ms, steps, launches, peak, peak_kind):
-    """Per launch: one pass over memory, which advances steps / launches time
-    steps (1 without temporal blocking); algorithmic bytes of a pass are
-    bytes_per_unit per cell (every cell read once and written once)."""
+    """Per launch, with the algorithmic bytes of a lattice-site update
+    (bytes_per_unit: one read and one write of every cell and step) times
+    the updates one launch performs: a launch that advances k time steps
+    (temporal blocking) performs k updates per cell.  frac above 1 is what
+    fusing steps buys: the pass moves each cell once for k updates, so the
+    per-pass figures (one read and one write per cell and launch, what HBM
+    actually sees) are reported beside it."""
     launch_ms = ms / max(1, launches)
-    algo_bytes = w.units * w.bytes_per_unit
+    steps_per_launch = steps / max(1, launches)
+    pass_bytes = w.units * w.bytes_per_unit
+    algo_bytes = pass_bytes * steps_per_launch
     achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4),
                 "peak_source": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured"
                 else "fallback 6800 GB/s",
                 "algorithmic_bytes_per_launch": int(algo_bytes), "launch_ms": round(launch_ms, 4),
-                "steps_per_launch": round(steps / max(1, launches), 3), "traffic": profile_traffic(w.traffic_key())}
+                "steps_per_launch": round(steps_per_launch, 3), "traffic": profile_traffic(w.traffic_key())}
     if launches and launches < steps:
-        # the same time with the algorithmic bytes of every time step (per
-        # lattice update: one read and one write per cell), i.e. the HBM
-        # bandwidth a one-step-per-pass code would need for this GLUPS
-        eff = w.units * w.bytes_per_unit * steps / (ms * 1e-3) / 1e9
-        roofline["effective_gbs_one_step_per_pass"] = round(eff, 1)
-        roofline["frac_one_step_per_pass"] = round(eff / peak, 4)
+        per_pass = pass_bytes / (launch_ms * 1e-3) / 1e9
+        roofline["per_pass_gbs"] = round(per_pass, 1)
+        roofline["frac_per_pass"] = round(per_pass / peak, 4)
+        roofline["per_pass_bytes"] = int(pass_bytes)
     return roofline
 
 
