@@ -197,14 +197,24 @@ def workload_config(name: str, args, world: int = 1) -> dict:
     else:
         raise ValueError(name)
     if world > 1:
-        cfg["parallelism"] = ("z-slabs, %d ranks" % world) if slab_capable(name) else ("replicas, %d ranks" % world)
+        if name == "gol_u8_8192":
+            cfg["parallelism"] = "y-slabs of 8192^2 cells, %d ranks" % world
+        elif slab_capable(name):
+            cfg["parallelism"] = "z-slabs, %d ranks" % world
+        elif name == "sell_f64_4m":
+            cfg["parallelism"] = "row blocks of whole chunks, an all-gather of the node values per step, %d ranks" % world
+        elif name == "lbm_d3q19_ensemble_512":
+            cfg["parallelism"] = "%d independent ensembles of %d cavities (seed 42 + rank), %d ranks" % (
+                world, getattr(args, "lbm_instances", 512), world)
+        else:
+            cfg["parallelism"] = "replicas, %d ranks" % world
     else:
         cfg["parallelism"] = "single GPU"
     return cfg
 
 
 def slab_capable(name: str) -> bool:
-    return name.startswith("jacobi7") or name == "varcoef_f32_256"
+    return name.startswith("jacobi7") or name in ("varcoef_f32_256", "gol_u8_8192")
 
 
 # ---------------------------------------------------------------- workloads
@@ -432,7 +442,7 @@ class LbmWorkload:
     run_steps = 500
     bytes_per_unit = 152     # 19 FP32 reads + 19 FP32 writes per cell
 
-    def __init__(self, instances=512, edge_max=192, tune=True, time_block=None):
+    def __init__(self, instances=512, edge_max=192, tune=True, time_block=None, seed=42):
         from libgeodecomp_gb300 import lgd, workloads
         self.lgd = lgd
         self.name = "lbm_d3q19_ensemble_512"
@@ -440,7 +450,7 @@ class LbmWorkload:
         self.unit = "GLUPS"
         # the configuration is 512 instances with edges up to 192; smaller
         # ensembles serve profiling captures
-        edges, omegas = workloads.lbm_ensemble(instances, seed=42, edge_max=edge_max)
+        edges, omegas = workloads.lbm_ensemble(instances, seed=seed, edge_max=edge_max)
         self.e = lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=4)
         self.units, self.items = self.e.info()
         t0 = time.perf_counter()
@@ -490,8 +500,10 @@ class LbmWorkload:
 def make_workload(name, args):
     if name == "lbm_d3q19_ensemble_512":
         tb = tuple(int(v) for v in args.lbm_time_block.split(",")) if args.lbm_time_block else None
+        # several GPUs: the ensemble's instances are independent, so every
+        # rank advances its own 512 cavities (seed 42 + rank), no collective
         return LbmWorkload(instances=args.lbm_instances, edge_max=args.lbm_edge_max, tune=not args.lbm_no_tune,
-                           time_block=tb)
+                           time_block=tb, seed=42 + getattr(args, "rank", 0))
     if name == "jacobi7_f64_512":
         return JacobiWorkload(ieee=False, edge=args.size)
     if name == "jacobi7_f64_ieee_512":
@@ -675,6 +687,9 @@ def run_gpu(args, world, rank, local, dist):
     peak, peak_kind = load_peaks()
     if world > 1 and slab_capable(args.workload):
         return run_slabs(args, world, rank, local, dist, peak, peak_kind)
+    if world > 1 and args.workload == "sell_f64_4m":
+        return run_sell_shards(args, world, rank, local, dist)
+    args.rank = rank
     w = make_workload(args.workload, args)
     if hasattr(w, "set_time_block"):
         w.set_time_block(args.time_block, args.time_block_shape)
@@ -769,12 +784,21 @@ def run_slabs(args, world, rank, local, dist, peak, peak_kind):
     import torch
     from libgeodecomp_gb300 import lgd, slabs
     cell = {"jacobi7_f64_512": lgd.CELL_JACOBI7_F64_FIX, "jacobi7_f64_ieee_512": lgd.CELL_JACOBI7_F64,
-            "jacobi7_f32_512": lgd.CELL_JACOBI7_F32, "varcoef_f32_256": lgd.CELL_VARCOEF_F32}[args.workload]
-    n = 256 if args.workload == "varcoef_f32_256" else args.size
+            "jacobi7_f32_512": lgd.CELL_JACOBI7_F32, "varcoef_f32_256": lgd.CELL_VARCOEF_F32,
+            "gol_u8_8192": lgd.CELL_GOL_U8}[args.workload]
+    n = {"varcoef_f32_256": 256, "gol_u8_8192": 8192}.get(args.workload, args.size)
     comm = slabs.TorchComm(dist, device=True)
-    s = slabs.SlabGrid(cell, (n * world, n, n), comm, periodic=7 if args.workload == "varcoef_f32_256" else 0,
-                       ghost=args.slab_ghost, time_block=args.time_block)
-    if args.workload == "varcoef_f32_256":
+    if args.workload == "gol_u8_8192":
+        # a torus of world slabs of 8192^2 cells, cut along y; ghost zones of
+        # 16 rows (one 16-generation pass between exchanges)
+        s = slabs.SlabGrid(cell, (n * world, n), comm, periodic=3, ghost=max(args.slab_ghost, 16),
+                           time_block=args.time_block)
+    else:
+        s = slabs.SlabGrid(cell, (n * world, n, n), comm, periodic=7 if args.workload == "varcoef_f32_256" else 0,
+                           ghost=args.slab_ghost, time_block=args.time_block)
+    if args.workload == "gol_u8_8192":
+        s.fill_bernoulli(0.3, seed=42)
+    elif args.workload == "varcoef_f32_256":
         from libgeodecomp_gb300 import workloads
         u0, kappa = workloads.varcoef_fields(n, seed=42, length=16.0)
         s.upload(0, np.concatenate([u0] * world).astype(np.float32))
@@ -793,7 +817,7 @@ def run_slabs(args, world, rank, local, dist, peak, peak_kind):
     torch.cuda.synchronize()
     barrier(dist)
     dt = max_over_ranks(dist, dt)
-    units = n * n * n
+    units = n * n if args.workload == "gol_u8_8192" else n * n * n
     value = units * world * args.steps / dt / 1e9
     launches = s.launch_count()
     if rank == 0:
@@ -807,6 +831,43 @@ def run_slabs(args, world, rank, local, dist, peak, peak_kind):
                 "slabs": s.describe(), "e2e": None, "cpu_baseline": None, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     s.close()
+    dist.destroy_process_group()
+
+
+def run_sell_shards(args, world, rank, local, dist):
+    """Strong scaling of the 4,194,304-node SELL-C-sigma diffusion over row
+    blocks: every rank updates its chunks and the ranks all-gather the new
+    node values every step (libgeodecomp_gb300.sell_shards)."""
+    import torch
+    from libgeodecomp_gb300 import lgd, sell_shards, slabs, workloads
+    n = SellWorkload.n
+    rp, col, w = workloads.powerlaw_graph(n, seed=42)
+    g = lgd.SellGrid.from_csr(n, rp, col, w, 32, 256)
+    g.upload(workloads.sell_values(n, seed=42))
+    s = sell_shards.ShardedSell(g, slabs.TorchComm(dist, device=True), 32)
+    s.step(args.warmup)
+    s.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        s.step(args.steps)
+        s.synchronize()
+        dt = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    barrier(dist)
+    dt = max_over_ranks(dist, dt)
+    if rank == 0:
+        line = {"metric": METRICS["sell_f64_4m"], "value": round(n * args.steps / dt / 1e9, 3), "unit": "GLUPS",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(dt * 1e3 / args.steps, 4), "s_per_step": round(dt / args.steps, 7),
+                "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded power-law graph and values)",
+                "config": workload_config("sell_f64_4m", args, world), "gpu_launches": args.steps,
+                "timing": "host clock around the ranks' steps (all-gathers included), max over ranks",
+                "row_blocks": s.describe(), "e2e": None, "cpu_baseline": None, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    g.close()
     dist.destroy_process_group()
 
 

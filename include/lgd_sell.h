@@ -98,6 +98,16 @@ int lgd_sell_step(lgd_sell *h, int count);
  * storage/unstructuredlooppeeler.h:75-126). */
 int lgd_sell_update_rows(lgd_sell *h, int row_begin, int row_end);
 int lgd_sell_swap(lgd_sell *h);
+
+/* Device address of node-value buffer which (0 current, 1 next): rows_padded
+ * values of the handle's precision in physical order (rows_padded = chunks
+ * x C; the padding rows hold 0).  For a row-block decomposition over ranks
+ * (each rank updates its chunks with lgd_sell_update_rows, the ranks gather
+ * every block of the next buffer, then lgd_sell_swap): what the reference's
+ * HiParSimulator would do with an unstructured grid's patch links
+ * (parallelization/hiparsimulator.h, communication/patchlink.h).  Work on the
+ * buffers must be ordered with the handle's stream. */
+int lgd_sell_x_device(lgd_sell *h, int which, void **ptr, int64_t *rows_padded);
 int lgd_sell_synchronize(lgd_sell *h);
 int lgd_sell_stream(lgd_sell *h, void **stream);
 int lgd_sell_launch_count(lgd_sell *h, uint64_t *count);

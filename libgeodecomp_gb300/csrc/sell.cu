@@ -878,6 +878,17 @@ int lgd_sell_swap(lgd_sell *h)
     });
 }
 
+int lgd_sell_x_device(lgd_sell *h, int which, void **ptr, int64_t *rows_padded)
+{
+    return guard([&] {
+        Sell& s = sell_of(h);
+        LGD_REQUIRE(which == 0 || which == 1, LGD_ERR_INVALID, "which must be 0 (current) or 1 (next)");
+        LGD_REQUIRE(ptr != nullptr, LGD_ERR_INVALID, "null output");
+        *ptr = which == 0 ? s.d_x[s.cur] : s.d_x[1 - s.cur];
+        if (rows_padded) *rows_padded = s.rows_padded;
+    });
+}
+
 int lgd_sell_synchronize(lgd_sell *h)
 {
     return guard([&] { LGD_CHECK_CUDA(cudaStreamSynchronize(sell_of(h).stream)); });

@@ -130,6 +130,7 @@ def lib():
             "lgd_sell_step": [P, I],
             "lgd_sell_update_rows": [P, I, I],
             "lgd_sell_swap": [P],
+            "lgd_sell_x_device": [P, I, P, P],
             "lgd_sell_synchronize": [P],
             "lgd_sell_stream": [P, P],
             "lgd_sell_launch_count": [P, P],
@@ -474,6 +475,13 @@ class SellGrid:
 
     def swap(self):
         check(lib().lgd_sell_swap(self._h))
+
+    def x_device(self, which: int = 0):
+        """(device address, rows_padded) of node-value buffer which (physical
+        order, the handle's precision)."""
+        p, n = ctypes.c_void_p(), ctypes.c_int64()
+        check(lib().lgd_sell_x_device(self._h, which, ctypes.byref(p), ctypes.byref(n)))
+        return p.value, n.value
 
     def synchronize(self):
         check(lib().lgd_sell_synchronize(self._h))

@@ -104,6 +104,10 @@ class TorchComm:
         for r in reqs:
             r.wait()
 
+    def allgather(self, send, recvs):
+        """recvs[q] <- rank q's send (equal sizes), every rank."""
+        self.dist.all_gather(recvs, send)
+
     def max_int(self, v: int) -> int:
         import torch
         t = torch.tensor([v], dtype=torch.int64, device="cuda" if self.device else "cpu")
@@ -157,6 +161,18 @@ class InProcessComm:
                     t[...] = msg
         self.hub.barrier.wait()
 
+    def allgather(self, send, recvs):
+        with self.hub.lock:
+            self.hub.box[("gather", self.rank)] = send.clone() if self.device else np.array(send, copy=True)
+        self.hub.barrier.wait()
+        for q in range(self.world):
+            msg = self.hub.box[("gather", q)]
+            if self.device:
+                recvs[q].copy_(msg)
+            else:
+                recvs[q][...] = msg
+        self.hub.barrier.wait()
+
     def _reduce(self, v, fn):
         with self.hub.lock:
             self.hub.box.setdefault("reduce", []).append(v)
@@ -198,7 +214,12 @@ class SlabGrid:
         world, rank = (comm.world, comm.rank) if comm is not None else (1, 0)
         self.layout = SlabLayout(shape[0], world, rank, ghost, bool(periodic & self.cut_bit))
         local_mask = periodic & ~self.cut_bit
-        if self.layout.local_periodic:
+        if periodic & self.cut_bit:
+            # one rank: the whole periodic axis wraps locally.  Several: every
+            # face of every slab is a ghost face, and what lies beyond a ghost
+            # zone never reaches the owned planes between two exchanges, so
+            # the local grid may wrap there too - which keeps the torus fast
+            # paths (Game of Life's bit-sliced passes, the var-coef TMA ring)
             local_mask |= self.cut_bit
         self.local_shape = (self.layout.local_planes,) + shape[1:]
         if make_grid is None:
@@ -261,6 +282,20 @@ class SlabGrid:
         out = np.empty((len(planes),) + self.shape[1:])
         for i, p in enumerate(planes):
             out[i] = workloads.uniform(seed, stream, n_plane, offset=int(p) * n_plane).reshape(self.shape[1:])
+        self.grid.upload(0, out)
+        self.since = self.period
+
+    def fill_bernoulli(self, p: float, seed: int = 42, stream: int = 1):
+        """Bernoulli(p) 0/1 cells of the global grid (value i = 1 if the
+        library's uniform i < p), each rank generating its own planes."""
+        from libgeodecomp_gb300 import workloads
+        n_plane = int(np.prod(self.shape[1:]))
+        g0, g1 = self.layout.global_range()
+        planes = np.arange(g0, g1) % self.shape[0]
+        out = np.empty((len(planes),) + self.shape[1:], dtype=np.uint8)
+        for i, q in enumerate(planes):
+            u = workloads.uniform(seed, stream, n_plane, offset=int(q) * n_plane)
+            out[i] = (u < p).astype(np.uint8).reshape(self.shape[1:])
         self.grid.upload(0, out)
         self.since = self.period
 
