@@ -589,6 +589,8 @@ def roofline_of(w, ms, steps, launches, peak, peak_kind):
         roofline["per_pass_gbs"] = round(per_pass, 1)
         roofline["frac_per_pass"] = round(per_pass / peak, 4)
         roofline["per_pass_bytes"] = int(pass_bytes)
+        roofline["note"] = ("temporal blocking: %.3g time steps per launch; achieved counts the bytes of every "
+                            "update, per_pass_gbs what HBM moves" % steps_per_launch)
     return roofline
 
 
