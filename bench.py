@@ -465,7 +465,7 @@ class LbmWorkload:
         self.depth = depth
         self.setup = {"cells": self.units, "work_items": self.items, "tune_s": round(time.perf_counter() - t0, 2),
                       "tuned_launch": {"tile_rows": ty, "threads": th, "ctas_per_sm": ct},
-                      "tuned_time_block": {"steps_per_launch": depth, "tile": "32x8" if shape == 0 else "32x4",
+                      "tuned_time_block": {"steps_per_launch": depth, "tile": ["32x8", "32x4"][shape],
                                            "ctas_per_sm": ctas}}
 
     def traffic_key(self):

@@ -67,7 +67,7 @@ struct Lbm {
     int variant;        // 0: plain loads and stores; 1: read-only-path loads, evict-first stores
     uint64_t launches;
     // temporal blocking: depth 1 (one step per launch) or 2 (lbm_tb2_kernel),
-    // tile shape 0 (32 x 8) or 1 (32 x 4), resident CTAs per SM of the
+    // column shape 0 (32 x 8) or 1 (32 x 4), resident CTAs per SM of the
     // depth-2 kernel; its work items are (instance, x0, y0) columns
     int depth;
     int tb_shape;
@@ -79,9 +79,21 @@ struct Lbm {
 
 // D3Q19 directions in the reference's naming order: C, N, E, W, S, T, B,
 // NW, SW, NE, SE, TW, BW, TE, BE, TN, BN, TS, BS (N = +y, E = +x, T = +z)
-__constant__ int c_ex[19] = {0, 0, 1, -1, 0, 0, 0, -1, -1, 1, 1, -1, -1, 1, 1, 0, 0, 0, 0};
-__constant__ int c_ey[19] = {0, 1, 0, 0, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1};
-__constant__ int c_ez[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+// (compile-time functions, so that unrolled loops fold them: a __constant__
+// table is a runtime value, and e * u would cost a conversion and a
+// multiplication per component)
+__host__ __device__ constexpr int dir_ex(int i)
+{
+    return (i == 2 || i == 9 || i == 10 || i == 13 || i == 14) ? 1 : (i == 3 || i == 7 || i == 8 || i == 11 || i == 12) ? -1 : 0;
+}
+__host__ __device__ constexpr int dir_ey(int i)
+{
+    return (i == 1 || i == 7 || i == 9 || i == 15 || i == 16) ? 1 : (i == 4 || i == 8 || i == 10 || i == 17 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int dir_ez(int i)
+{
+    return (i == 5 || i == 11 || i == 13 || i == 15 || i == 17) ? 1 : (i == 6 || i == 12 || i == 14 || i == 16 || i == 18) ? -1 : 0;
+}
 
 template<int I> struct Q;
 #define LGD_Q(I, EX, EY, EZ, OPP) \
@@ -106,6 +118,18 @@ LGD_Q(16, 0, 1, -1, 17)
 LGD_Q(17, 0, -1, 1, 16)
 LGD_Q(18, 0, -1, -1, 15)
 #undef LGD_Q
+
+template<int I>
+struct DirCheck {
+    static_assert(dir_ex(I) == Q<I>::ex && dir_ey(I) == Q<I>::ey && dir_ez(I) == Q<I>::ez, "direction tables agree");
+    static_assert(Q<Q<I>::opp>::opp == I && Q<Q<I>::opp>::ex == -Q<I>::ex, "opposite directions");
+    static const bool ok = DirCheck<I - 1>::ok;
+};
+template<>
+struct DirCheck<-1> {
+    static const bool ok = true;
+};
+static_assert(DirCheck<18>::ok, "D3Q19 tables");
 
 template<typename R>
 struct LbmArith;
@@ -184,6 +208,15 @@ struct PullAll<R, 19, IDX, NC, INTERIOR> {
 
 // BGK collision, operation order of the oracle's lgd_d3q19_collide; put(i,
 // v) stores post-collision population i
+// e * u for a direction component e in {-1, 0, 1} known at compile time:
+// u, -u, or u * 0 (kept as a multiplication, so that the sign of a zero
+// product is the IEEE product's) - bit for bit the product (R)e * u
+template<typename R>
+__device__ __forceinline__ R mul_dir(int e, R u)
+{
+    return e == 1 ? u : (e == -1 ? -u : LbmArith<R>::mul((R)0, u));
+}
+
 template<typename R, typename PUT>
 __device__ __forceinline__ void collide_to(const R *f, R omega, PUT put)
 {
@@ -209,7 +242,7 @@ __device__ __forceinline__ void collide_to(const R *f, R omega, PUT put)
 #pragma unroll
     for (int i = 1; i < 19; ++i) {
         // eu = ex * ux + ey * uy + ez * uz, evaluated as the oracle does
-        const R eu = A::add(A::add(A::mul((R)c_ex[i], ux), A::mul((R)c_ey[i], uy)), A::mul((R)c_ez[i], uz));
+        const R eu = A::add(A::add(mul_dir<R>(dir_ex(i), ux), mul_dir<R>(dir_ey(i), uy)), mul_dir<R>(dir_ez(i), uz));
         const R wi = (i < 7) ? w1 : w2;
         put(i, A::add(A::mul(keep, f[i]), A::mul(wi, A::add(A::add(d, eu), A::mul((R)1.5, A::mul(eu, eu))))));
     }
@@ -519,30 +552,35 @@ static const void *tb2_fn()
     return (const void *)lbm_tb2_kernel<R, IDX, TX, TY>;
 }
 
-template<typename R, int TX, int TY>
-static const void *tb2_fn_idx(const Lbm& e)
+template<int TX, int TY>
+static const void *tb2_geo(const Lbm& e, int *threads, size_t *smem)
 {
-    return e.idx32 ? tb2_fn<R, int, TX, TY>() : tb2_fn<R, long long, TX, TY>();
+    typedef Tb2Geo<TX, TY> G;
+    *threads = G::THREADS;
+    *smem = e.precision == 4 ? G::template smem<float>() : G::template smem<double>();
+    if (e.precision == 4) return e.idx32 ? tb2_fn<float, int, TX, TY>() : tb2_fn<float, long long, TX, TY>();
+    return e.idx32 ? tb2_fn<double, int, TX, TY>() : tb2_fn<double, long long, TX, TY>();
 }
 
-// the depth-2 kernel of the ensemble's precision, index width and shape,
-// its threads per CTA and shared memory per CTA
+// the column shapes of the depth-2 kernel: 0 = 32 x 8, 1 = 32 x 4 (64 x 4
+// and 16 x 8 columns measured slower on the 512-cavity ensemble: 33.0 and
+// 25.1 GLUPS at their best residency, against 35.6 and 38.5)
+constexpr int TB2_SHAPES = 2;
+static int tb2_tx(int) { return 32; }
+static int tb2_ty(int shape) { return shape == 1 ? 4 : 8; }
+
+// the depth-2 kernel of the ensemble's precision, index width and column
+// shape, its threads per CTA and shared memory per CTA
 static const void *tb2_kernel(const Lbm& e, int shape, int *threads, size_t *smem)
 {
-    if (shape == 1) {
-        *threads = Tb2Geo<32, 4>::THREADS;
-        *smem = e.precision == 4 ? Tb2Geo<32, 4>::smem<float>() : Tb2Geo<32, 4>::smem<double>();
-        return e.precision == 4 ? tb2_fn_idx<float, 32, 4>(e) : tb2_fn_idx<double, 32, 4>(e);
-    }
-    *threads = Tb2Geo<32, 8>::THREADS;
-    *smem = e.precision == 4 ? Tb2Geo<32, 8>::smem<float>() : Tb2Geo<32, 8>::smem<double>();
-    return e.precision == 4 ? tb2_fn_idx<float, 32, 8>(e) : tb2_fn_idx<double, 32, 8>(e);
+    if (shape == 1) return tb2_geo<32, 4>(e, threads, smem);
+    return tb2_geo<32, 8>(e, threads, smem);
 }
 
 // column work items of a depth-2 tile shape, largest instances first
 static void build_cols(Lbm& e, int shape)
 {
-    const int TX = 32, TY = shape == 1 ? 4 : 8;
+    const int TX = tb2_tx(shape), TY = tb2_ty(shape);
     std::vector<int> order(e.count);
     for (int j = 0; j < e.count; ++j) order[j] = j;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e.inst[a].L > e.inst[b].L; });
@@ -876,12 +914,12 @@ int lgd_lbm_tune(lgd_lbm *h, int trial_steps, int *tile_rows, int *threads, int 
         // misc/cacheblockingsimulationfactory.h:26-28)
         e.depth = 1;
         int best_depth = 1, best_shape = 0, best_ctas = 1;
-        for (int shape = 0; shape < 2; ++shape) {
+        for (int shape = 0; shape < TB2_SHAPES; ++shape) {
             int threads = 0;
             size_t smem = 0;
             const void *fn = tb2_kernel(e, shape, &threads, &smem);
             const int per_sm = tb2_resident(fn, threads, smem);
-            for (int ct = 1; ct <= std::min(per_sm, 4); ++ct) {
+            for (int ct = 1; ct <= std::min(per_sm, 8); ++ct) {
                 e.depth = 2;
                 e.tb_shape = shape;
                 e.tb_ctas = ct;
@@ -920,7 +958,8 @@ int lgd_lbm_set_time_block(lgd_lbm *h, int depth, int shape, int ctas_per_sm)
     return guard([&] {
         Lbm& e = lbm_of(h);
         LGD_REQUIRE(depth == 1 || depth == 2, LGD_ERR_INVALID, "the ensemble fuses one or two steps per launch");
-        LGD_REQUIRE(shape == 0 || shape == 1, LGD_ERR_INVALID, "tile shape must be 0 (32 x 8) or 1 (32 x 4)");
+        LGD_REQUIRE(shape >= 0 && shape < TB2_SHAPES, LGD_ERR_INVALID,
+                    "column shape must be 0 (32 x 8) or 1 (32 x 4)");
         LGD_REQUIRE(ctas_per_sm >= 1 && ctas_per_sm <= 32, LGD_ERR_INVALID, "CTAs per SM out of range");
         if (depth == 2) {
             int threads = 0;

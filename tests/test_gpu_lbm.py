@@ -120,7 +120,7 @@ def test_lbm_upload_roundtrip_and_errors():
 
 
 # ----------------------------------------------- two steps per launch
-@pytest.mark.parametrize("shape,ctas", [(0, 1), (0, 2), (1, 1), (1, 3)])
+@pytest.mark.parametrize("shape,ctas", [(0, 1), (0, 2), (1, 1), (1, 3), (1, 4)])
 @pytest.mark.parametrize("steps", [10, 11])
 def test_lbm_two_steps_per_launch_bit_identical_fp64(shape, ctas, steps):
     """Depth 2 (the first step's populations of a column and its rim in
@@ -142,7 +142,7 @@ def test_lbm_two_steps_per_launch_bit_identical_fp64(shape, ctas, steps):
 def test_lbm_two_steps_fp32_equal_single_steps_and_reference_L24():
     edges, omegas = workloads.lbm_ensemble(20, seed=5, edge_min=6, edge_max=70)
     with lgd.LbmEnsemble(edges, omegas, precision=4) as a, lgd.LbmEnsemble(edges, omegas, precision=4) as b:
-        a.set_time_block(2, 0, 2)
+        a.set_time_block(2, 1, 4)
         a.step(8)
         b.step(8)
         for j in range(len(edges)):
