@@ -943,7 +943,9 @@ def run_reference(args, world, rank):
     line = {
         "metric": METRICS.get(args.workload, JACOBI_METRIC), "value": round(value, 4), "unit": "GLUPS",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPES.get(args.workload, "f64"),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (IEEE, the reference's cell arithmetic)" if args.workload.startswith("jacobi7_f64")
+        else DTYPES.get(args.workload, "f64"),
         "data": "synthetic (seeded SplitMix64, generated on device or by libgeodecomp_gb300.workloads)",
         "config": workload_config(args.workload, args, world),
         "impl": "reference",
