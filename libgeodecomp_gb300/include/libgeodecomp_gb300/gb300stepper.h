@@ -93,7 +93,11 @@ public:
             owned = CoordBox<DIM>(origin, dim);
             hostGrid = new HostGrid(owned);
             init->grid(hostGrid);
-            createDevice(wraps && ranks == 1);
+            // a wrapping cut axis wraps locally too: with one rank it is the
+            // whole axis; with several every face is a ghost face, and what
+            // lies beyond a ghost zone never reaches the owned planes
+            // between two exchanges, so the torus fast paths stay in use
+            createDevice(wraps);
             upload();
         } catch (...) {
             if (handle) lgd_gpu_destroy(handle);
