@@ -161,3 +161,24 @@ def test_lbm_512_ensemble_fp32_error_at_500_steps():
         max_abs = float(np.max(np.abs(got[j] - ref)))
         print("cavity %d (L = %d, omega %.3f): rel-L2 %.3g, max-abs %.3g" % (j, edges[j], omegas[j], rel_l2, max_abs))
         assert rel_l2 < 2e-4 and max_abs < 2e-4, (j, rel_l2, max_abs)
+
+
+def test_varcoef_256_full_run():
+    """The variable-coefficient configuration: 256^3 torus, GRF fields
+    (length 16), to t = 4096.  The FP64 cell is bit-identical to the oracle
+    over the whole run; the FP32 cell (the benchmarked one, packed FP32
+    arithmetic) stays within rel-L2 1e-5 of it (measured on GB300: 5.6e-6)."""
+    u0, k = workloads.varcoef_fields(256, seed=42, length=16.0)
+    ref = oracle.varcoef(u0, k, 4096)
+    with lgd.Grid(lgd.CELL_VARCOEF_F64, u0.shape, periodic=7) as g:
+        g.upload(0, u0)
+        g.upload(1, k)
+        g.step(4096)
+        np.testing.assert_array_equal(g.download(0), ref)
+    with lgd.Grid(lgd.CELL_VARCOEF_F32, u0.shape, periodic=7) as g:
+        g.upload(0, u0.astype(np.float32))
+        g.upload(1, k.astype(np.float32))
+        g.step(4096)
+        out = g.download(0).astype(np.float64)
+    rel_l2 = float(np.linalg.norm(out - ref) / np.linalg.norm(ref))
+    assert rel_l2 < 1e-5, rel_l2
