@@ -2,7 +2,8 @@
  * lgd_ensemble.h - C ABI for batched ensembles of independent grids.
  *
  * An ensemble of D3Q19 BGK lid-driven cavities of uneven sizes advanced by
- * one persistent kernel launch per time step, replayed from a CUDA graph.
+ * one persistent kernel launch per time step or per two time steps
+ * (temporal blocking), replayed from CUDA graphs.
  * The reference has no ensemble runner; the per-instance semantics are
  * those of one Simulator per grid (parallelization/serialsimulator.h:
  * 76-139) running a D3Q19 cell (collision of

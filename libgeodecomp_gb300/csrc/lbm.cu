@@ -12,7 +12,9 @@
 // instance, largest instances first - from an atomic counter until the list
 // is exhausted, so instances of 32^3 and 192^3 cells share the GPU without
 // per-instance launches.  Two steps (A -> B, B -> A, each with its counter
-// reset) are captured once into a CUDA graph and replayed.
+// reset) are captured once into a CUDA graph and replayed.  With temporal
+// blocking (lbm_tb2_kernel) one persistent launch advances two steps, and
+// two such launches (four steps) are captured and replayed the same way.
 //
 // Cell update (pull scheme, the reference LBM example's incompressible BGK
 // collision, src/examples/latticeboltzmann/main.cpp:93-170): population i
@@ -63,6 +65,12 @@ struct Lbm {
     cudaStream_t stream;
     cudaGraphExec_t graph;
     bool graph_valid;
+    // four steps of the depth-2 path (two two-step launches, 0 -> 1 -> 0)
+    // replayed from a graph; rebuilt when the form, residency or columns change
+    cudaGraphExec_t graph2;
+    bool graph2_valid;
+    int graph2_key[2];
+    const int4 *graph2_cols;
     bool idx32;         // every instance indexable with 32 bits (19 L^3 < 2^31)
     int variant;        // 0: plain loads and stores; 1: read-only-path loads, evict-first stores
     uint64_t launches;
@@ -618,15 +626,24 @@ static int tb2_resident(const void *fn, int threads, size_t smem)
     return per_sm;
 }
 
-// two steps of every instance in one launch (src -> 1 - src)
+// two steps of every instance in one launch (src -> 1 - src); with
+// capturing set the caller is capturing the stream, so nothing here may
+// allocate (prepare_tb2 first)
+static void prepare_tb2(Lbm& e)
+{
+    int threads = 0;
+    size_t smem = 0;
+    const void *fn = tb2_kernel(e, e.tb_shape, &threads, &smem);
+    LGD_REQUIRE(tb2_resident(fn, threads, smem) >= 1, LGD_ERR_UNSUPPORTED, "the two-step kernel does not fit on this GPU");
+    if (e.cols_shape != e.tb_shape || e.d_cols == nullptr) build_cols(e, e.tb_shape);
+}
+
 static void launch_tb2(Lbm& e, int src)
 {
     int threads = 0;
     size_t smem = 0;
     const void *fn = tb2_kernel(e, e.tb_shape, &threads, &smem);
     const int per_sm = tb2_resident(fn, threads, smem);
-    LGD_REQUIRE(per_sm >= 1, LGD_ERR_UNSUPPORTED, "the two-step kernel does not fit on this GPU");
-    if (e.cols_shape != e.tb_shape || e.d_cols == nullptr) build_cols(e, e.tb_shape);
     LGD_CHECK_CUDA(cudaMemsetAsync(e.d_counter + 2, 0, sizeof(int), e.stream));
     const int grid = e.sms * std::min(std::max(1, e.tb_ctas), per_sm);
     int *counter = e.d_counter + 2;
@@ -634,6 +651,35 @@ static void launch_tb2(Lbm& e, int src)
     void *b = e.buf[1 - src];
     void *args[] = {&e.d_inst, &e.d_cols, &e.n_cols, &counter, &a, &b};
     LGD_CHECK_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, e.stream));
+}
+
+static void rebuild_graph2(Lbm& e)
+{
+    prepare_tb2(e);
+    if (e.graph2_valid && e.graph2_key[0] == e.tb_shape && e.graph2_key[1] == e.tb_ctas && e.graph2_cols == e.d_cols) {
+        return;
+    }
+    if (e.graph2_valid) {
+        cudaGraphExecDestroy(e.graph2);
+        e.graph2_valid = false;
+    }
+    cudaGraph_t g;
+    LGD_CHECK_CUDA(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        launch_tb2(e, 0);
+        launch_tb2(e, 1);
+    } catch (...) {
+        cudaStreamEndCapture(e.stream, &g);
+        throw;
+    }
+    LGD_CHECK_CUDA(cudaStreamEndCapture(e.stream, &g));
+    cudaError_t err = cudaGraphInstantiate(&e.graph2, g, 0);
+    cudaGraphDestroy(g);
+    LGD_CHECK_CUDA(err);
+    e.graph2_valid = true;
+    e.graph2_key[0] = e.tb_shape;
+    e.graph2_key[1] = e.tb_ctas;
+    e.graph2_cols = e.d_cols;
 }
 
 static void launch_single(Lbm& e, int j, dim3 grid)
@@ -689,7 +735,20 @@ static void set_config(Lbm& e, int ty, int threads, int ctas)
 static void run_steps(Lbm& e, int steps)
 {
     if (e.depth == 2) {
-        // pairs of steps in one launch each, a last odd step on its own
+        // pairs of steps in one launch each (four steps per graph replay
+        // from buffer 0), a last odd step on its own
+        prepare_tb2(e);
+        if (e.cur == 1 && steps >= 2) {
+            launch_tb2(e, 1);
+            ++e.launches;
+            e.cur = 0;
+            steps -= 2;
+        }
+        if (steps >= 4) rebuild_graph2(e);
+        for (; steps >= 4; steps -= 4) {
+            LGD_CHECK_CUDA(cudaGraphLaunch(e.graph2, e.stream));
+            e.launches += 2;
+        }
         for (; steps >= 2; steps -= 2) {
             launch_tb2(e, e.cur);
             ++e.launches;
@@ -724,6 +783,7 @@ static void lbm_free(Lbm& e)
 {
     if (e.stream) cudaStreamSynchronize(e.stream);
     if (e.graph_valid) cudaGraphExecDestroy(e.graph);
+    if (e.graph2_valid) cudaGraphExecDestroy(e.graph2);
     cudaFree(e.buf[0]);
     cudaFree(e.buf[1]);
     cudaFree(e.d_inst);

@@ -121,7 +121,7 @@ def test_lbm_upload_roundtrip_and_errors():
 
 # ----------------------------------------------- two steps per launch
 @pytest.mark.parametrize("shape,ctas", [(0, 1), (0, 2), (1, 1), (1, 3), (1, 4)])
-@pytest.mark.parametrize("steps", [10, 11])
+@pytest.mark.parametrize("steps", [10, 11, 13])
 def test_lbm_two_steps_per_launch_bit_identical_fp64(shape, ctas, steps):
     """Depth 2 (the first step's populations of a column and its rim in
     shared memory) equals single steps and the oracle bit for bit: uneven
@@ -137,6 +137,23 @@ def test_lbm_two_steps_per_launch_bit_identical_fp64(shape, ctas, steps):
         assert e.time_block() == (2, shape, ctas)
         for j, (L, om) in enumerate(zip(edges, omegas)):
             np.testing.assert_array_equal(e.download(j), oracle.lbm(L, steps, om, 0.05), err_msg=str(j))
+
+
+def test_lbm_two_steps_graph_replay_across_uneven_calls():
+    """Calls of 3, 9, 6 and 4 steps: the four-step graph replays start from
+    either buffer (an odd call leaves the ensemble on the other one), and a
+    change of form or residency between calls rebuilds the graph."""
+    edges = [9, 33, 4, 20]
+    omegas = [1.1, 1.7, 0.9, 1.45]
+    with lgd.LbmEnsemble(edges, omegas, lid=0.05, precision=8) as e:
+        e.set_time_block(2, 1, 2)
+        for n in (3, 9):
+            e.step(n)
+        e.set_time_block(2, 0, 1)
+        for n in (6, 4):
+            e.step(n)
+        for j, (L, om) in enumerate(zip(edges, omegas)):
+            np.testing.assert_array_equal(e.download(j), oracle.lbm(L, 22, om, 0.05), err_msg=str(j))
 
 
 def test_lbm_two_steps_fp32_equal_single_steps_and_reference_L24():
