@@ -167,6 +167,21 @@ private:
     // cells of one plane of the cut axis
     std::size_t planeCells() const { return (std::size_t)global[0] * (DIM == 3 ? global[1] : 1); }
 
+    // rows of the owned box in the host grid, which stores x fastest (the
+    // reference's DisplacedGrid): row r starts at rowPointer(r), nx cells
+    std::size_t ownedRows() const
+    {
+        return (std::size_t)owned.dimensions[1] * (DIM == 3 ? (std::size_t)owned.dimensions[2] : 1);
+    }
+
+    CELL *rowPointer(std::size_t r)
+    {
+        Coord<DIM> c = owned.origin;
+        c[1] += (int)(r % (std::size_t)owned.dimensions[1]);
+        if (DIM == 3) c[2] += (int)(r / (std::size_t)owned.dimensions[1]);
+        return &(*hostGrid)[c];
+    }
+
     void createDevice(bool cutAxisWraps)
     {
         lgd_grid_desc d;
@@ -195,12 +210,16 @@ private:
     void upload()
     {
         const std::size_t cells = planeCells() * (std::size_t)localPlanes();
+        const std::size_t nx = (std::size_t)owned.dimensions[0];
         if (Traits::KIND == LGD_CELL_JACOBI7_F64_FIX) {
             double m = 0.0;
-            for (typename CoordBox<DIM>::Iterator i = owned.begin(); i != owned.end(); ++i) {
-                double v;
-                Traits::pack((*hostGrid)[*i], 0, &v);
-                m = std::max(m, std::fabs(v));
+            for (std::size_t r = 0; r < ownedRows(); ++r) {
+                const CELL *row = rowPointer(r);
+                for (std::size_t x = 0; x < nx; ++x) {
+                    double v;
+                    Traits::pack(row[x], 0, &v);
+                    m = std::max(m, std::fabs(v));
+                }
             }
             m = link ? link->maxOverRanks(m) : m;
             int e = 0;
@@ -211,8 +230,14 @@ private:
             const std::size_t sz = Traits::memberSize(m);
             std::vector<char> buf(cells * sz);
             char *dst = buf.data() + (std::size_t)ghostLo * planeCells() * sz;
-            for (typename CoordBox<DIM>::Iterator i = owned.begin(); i != owned.end(); ++i, dst += sz) {
-                Traits::pack((*hostGrid)[*i], m, dst);
+            for (std::size_t r = 0; r < ownedRows(); ++r) {
+                const CELL *row = rowPointer(r);
+                if (Traits::KIND == LGD_CELL_RECORD) {
+                    std::memcpy(dst, static_cast<const void *>(row), nx * sizeof(CELL));
+                    dst += nx * sizeof(CELL);
+                } else {
+                    for (std::size_t x = 0; x < nx; ++x, dst += sz) Traits::pack(row[x], m, dst);
+                }
             }
             gb300Check(lgd_gpu_upload(handle, m, 0, buf.data(), buf.size()));
         }
@@ -227,8 +252,15 @@ private:
             std::vector<char> buf(cells * sz);
             gb300Check(lgd_gpu_download(handle, m, 0, buf.data(), buf.size()));
             const char *src = buf.data() + (std::size_t)ghostLo * planeCells() * sz;
-            for (typename CoordBox<DIM>::Iterator i = owned.begin(); i != owned.end(); ++i, src += sz) {
-                Traits::unpack(&(*hostGrid)[*i], m, src);
+            const std::size_t nx = (std::size_t)owned.dimensions[0];
+            for (std::size_t r = 0; r < ownedRows(); ++r) {
+                CELL *row = rowPointer(r);
+                if (Traits::KIND == LGD_CELL_RECORD) {
+                    std::memcpy(static_cast<void *>(row), src, nx * sizeof(CELL));
+                    src += nx * sizeof(CELL);
+                } else {
+                    for (std::size_t x = 0; x < nx; ++x, src += sz) Traits::unpack(&row[x], m, src);
+                }
             }
         }
     }
