@@ -269,6 +269,12 @@ class Grid:
     def synchronize(self):
         check(lib().lgd_gpu_synchronize(self._h))
 
+    def stream(self) -> int:
+        """The handle's CUDA stream (a cudaStream_t) as an integer."""
+        p = ctypes.c_void_p()
+        check(lib().lgd_gpu_stream(self._h, ctypes.byref(p)))
+        return p.value
+
     def device_ptr(self, member: int = 0, which: int = 0):
         p = ctypes.c_void_p()
         pitch = ctypes.c_size_t()
