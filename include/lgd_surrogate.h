@@ -41,6 +41,13 @@ int lgd_net_set_params(lgd_net *h, const float *host, size_t count);
 int lgd_net_get_params(lgd_net *h, float *host, size_t count);
 int lgd_net_get_grads(lgd_net *h, float *host, size_t count);
 
+/* Replaces the gradient of the last backward pass (FP32, the parameter
+ * layout).  Data-parallel training: every rank runs forward and backward
+ * on its own batch, the ranks average their gradients (an all-reduce) and
+ * set the average before lgd_net_adam, so every rank takes the same step
+ * and the replicas stay identical. */
+int lgd_net_set_grads(lgd_net *h, const float *host, size_t count);
+
 /* d_du = net(u, kappa) (the increment; u' = u + d_du). */
 int lgd_net_forward(lgd_net *h, const float *d_u, const float *d_kappa, float *d_du);
 

@@ -925,6 +925,17 @@ int lgd_net_get_grads(lgd_net *h, float *host, size_t count)
     });
 }
 
+int lgd_net_set_grads(lgd_net *h, const float *host, size_t count)
+{
+    return guard([&] {
+        Net& n = net_of(h);
+        LGD_REQUIRE(n.training, LGD_ERR_INVALID, "network was created without training buffers");
+        LGD_REQUIRE(host != nullptr && (long long)count == n.P, LGD_ERR_INVALID, "parameter count mismatch");
+        LGD_CHECK_CUDA(cudaMemcpyAsync(n.grads, host, sizeof(float) * count, cudaMemcpyHostToDevice, n.stream));
+        LGD_CHECK_CUDA(cudaStreamSynchronize(n.stream));
+    });
+}
+
 int lgd_net_forward(lgd_net *h, const float *d_u, const float *d_kappa, float *d_du)
 {
     return guard([&] {

@@ -108,6 +108,15 @@ class TorchComm:
         """recvs[q] <- rank q's send (equal sizes), every rank."""
         self.dist.all_gather(recvs, send)
 
+    def allreduce_mean(self, a: np.ndarray) -> np.ndarray:
+        """The mean over ranks of a host array, on every rank."""
+        import torch
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        if self.device:
+            t = t.cuda()
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return (t.cpu().numpy() / self.world).astype(a.dtype)
+
     def max_int(self, v: int) -> int:
         import torch
         t = torch.tensor([v], dtype=torch.int64, device="cuda" if self.device else "cpu")
@@ -172,6 +181,15 @@ class InProcessComm:
             else:
                 recvs[q][...] = msg
         self.hub.barrier.wait()
+
+    def allreduce_mean(self, a: np.ndarray) -> np.ndarray:
+        """The mean over ranks of a host array, summed in rank order."""
+        parts = [p for _, p in sorted(self._reduce((self.rank, np.array(a, copy=True)), list),
+                                      key=lambda rp: rp[0])]
+        acc = parts[0].copy()
+        for p in parts[1:]:
+            acc = acc + p
+        return (acc / self.world).astype(a.dtype)
 
     def _reduce(self, v, fn):
         with self.hub.lock:

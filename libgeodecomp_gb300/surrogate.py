@@ -39,6 +39,7 @@ def _bind():
         "lgd_net_set_params": [P, P, ctypes.c_size_t],
         "lgd_net_get_params": [P, P, ctypes.c_size_t],
         "lgd_net_get_grads": [P, P, ctypes.c_size_t],
+        "lgd_net_set_grads": [P, P, ctypes.c_size_t],
         "lgd_net_forward": [P, P, P, P],
         "lgd_net_backward": [P, P, P],
         "lgd_net_adam": [P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float],
@@ -116,6 +117,11 @@ class SurrogateNet:
         a = np.empty(self.P, dtype=np.float32)
         lgd.check(self._L.lgd_net_get_grads(self._h, a.ctypes.data, a.size))
         return a
+
+    def set_grads(self, g: np.ndarray):
+        a = np.ascontiguousarray(g, dtype=np.float32)
+        assert a.size == self.P
+        lgd.check(self._L.lgd_net_set_grads(self._h, a.ctypes.data, a.size))
 
     def forward(self, u, kappa, du):
         lgd.check(self._L.lgd_net_forward(self._h, u.data_ptr(), kappa.data_ptr(), du.data_ptr()))
@@ -230,11 +236,19 @@ def make_trajectories(count: int = 2000, n: int = 32, calls: int = 4, length: fl
 
 
 def train(states, kappa, channels: int = 24, iters: int = 1500, batch: int = 8, lr: float = 1e-3, seed: int = 0,
-          params: np.ndarray | None = None, log=None):
+          params: np.ndarray | None = None, log=None, comm=None):
     """Adam on the MSE of the one-call increment over random (trajectory,
-    call) pairs; returns (params, loss history)."""
+    call) pairs; returns (params, loss history).
+
+    comm (a libgeodecomp_gb300.slabs comm, several ranks): data-parallel
+    training.  Every rank draws the same global batch of world x batch
+    pairs and trains on its own slice; the ranks average their gradients
+    (one all-reduce per iteration) before the Adam step, so the replicas
+    stay identical and follow the single-rank run with the global batch
+    (up to the order of the FP32 gradient sums)."""
     import torch
     count, calls1, n = states.shape[0], states.shape[1], states.shape[2]
+    world, rank = (comm.world, comm.rank) if comm is not None else (1, 0)
     rng = np.random.default_rng(seed)
     net = SurrogateNet((n, n, n), batch=batch, channels=channels, training=True)
     net.set_params(init_params(channels, seed) if params is None else params)
@@ -245,8 +259,8 @@ def train(states, kappa, channels: int = 24, iters: int = 1500, batch: int = 8, 
     hist = []
     try:
         for it in range(iters):
-            j = rng.integers(0, count, batch)
-            c = rng.integers(0, calls1 - 1, batch)
+            j = rng.integers(0, count, batch * world)[rank * batch:(rank + 1) * batch]
+            c = rng.integers(0, calls1 - 1, batch * world)[rank * batch:(rank + 1) * batch]
             ji = torch.as_tensor(j, device="cuda")
             ci = torch.as_tensor(c, device="cuda")
             u.copy_(states[ji, ci])
@@ -255,6 +269,9 @@ def train(states, kappa, channels: int = 24, iters: int = 1500, batch: int = 8, 
             torch.cuda.synchronize()
             net.forward(u, k, du)
             loss = net.backward(tgt)
+            if world > 1:
+                net.set_grads(comm.allreduce_mean(net.get_grads()))
+                loss = float(comm.allreduce_mean(np.array([loss]))[0])
             net.adam(lr=lr * (0.1 if it > 0.8 * iters else 1.0))
             hist.append(loss)
             if log and (it % 100 == 0 or it == iters - 1):

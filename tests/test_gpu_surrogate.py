@@ -121,6 +121,44 @@ def test_training_lowers_loss_and_beats_the_no_learning_baseline():
     assert err_net < 0.5 * err_id, (err_net, err_id)
 
 
+def test_data_parallel_training_follows_the_global_batch():
+    """Two ranks (threads of one process, each its own network on the GPU)
+    train on halves of the same global batch and average their gradients
+    before every Adam step: both replicas end bit-identical, and equal to
+    one network trained on the whole batch up to the order of the FP32
+    gradient sums."""
+    import threading
+    from libgeodecomp_gb300 import slabs
+    from libgeodecomp_gb300 import surrogate as S
+    states, kappa = S.make_trajectories(count=16, n=32, calls=3, length=8.0, seed=5)
+    p0 = S.init_params(24, seed=2)
+    single, hist1 = S.train(states, kappa, channels=24, iters=6, batch=4, lr=1e-3, seed=4, params=p0)
+    hub = slabs.InProcessComm.Hub(2)
+    out = [None, None]
+    errors = []
+
+    def rank_main(r):
+        try:
+            out[r] = S.train(states, kappa, channels=24, iters=6, batch=2, lr=1e-3, seed=4, params=p0,
+                             comm=slabs.InProcessComm(hub, r))
+        except Exception as e:
+            errors.append(e)
+            hub.barrier.abort()
+
+    threads = [threading.Thread(target=rank_main, args=(r,)) for r in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    (pa, ha), (pb, hb) = out
+    np.testing.assert_array_equal(pa, pb)
+    assert ha == hb
+    np.testing.assert_allclose(pa, single, rtol=1e-3, atol=1e-5)
+    np.testing.assert_allclose(ha, hist1, rtol=1e-3)
+    assert not np.array_equal(pa, p0)
+
+
 def test_judge_falls_back_to_the_plain_stencil():
     from libgeodecomp_gb300 import surrogate as S
     n = 32

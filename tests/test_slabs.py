@@ -231,3 +231,52 @@ def test_two_gloo_ranks_exchange_through_host_buffers(mask):
         assert p.returncode == 0, err[-3000:]
     line = json.loads(outs[0][0].strip().splitlines()[-1])
     assert line["equal"] and line["exchanges"] >= 6
+
+
+def test_in_process_allreduce_mean_is_identical_on_every_rank():
+    world = 3
+    hub = slabs.InProcessComm.Hub(world)
+    out = [None] * world
+
+    def rank_main(r):
+        comm = slabs.InProcessComm(hub, r)
+        out[r] = comm.allreduce_mean(np.arange(5, dtype=np.float32) * (r + 1))
+
+    threads = [threading.Thread(target=rank_main, args=(r,)) for r in range(world)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for o in out:
+        np.testing.assert_array_equal(o, out[0])
+    np.testing.assert_allclose(out[0], np.arange(5) * 2.0)
+    assert out[0].dtype == np.float32
+
+
+REDUCE_WORKER = r"""
+import sys, json
+sys.path.insert(0, {root!r})
+import numpy as np
+import torch.distributed as dist
+from libgeodecomp_gb300 import slabs
+dist.init_process_group("gloo")
+comm = slabs.TorchComm(dist, device=False)
+m = comm.allreduce_mean(np.arange(4, dtype=np.float32) + 10 * comm.rank)
+print(json.dumps({{"rank": comm.rank, "mean": m.tolist(), "dtype": str(m.dtype)}}))
+dist.destroy_process_group()
+"""
+
+
+def test_two_gloo_ranks_average_an_array():
+    port = free_port()
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE="2", MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, "-c", REDUCE_WORKER.format(root=ROOT)], env=env,
+                                      stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
+    outs = [p.communicate(timeout=300) for p in procs]
+    for p, (out, err) in zip(procs, outs):
+        assert p.returncode == 0, err[-3000:]
+        line = json.loads(out.strip().splitlines()[-1])
+        assert line["mean"] == [5.0, 6.0, 7.0, 8.0] and line["dtype"] == "float32"
