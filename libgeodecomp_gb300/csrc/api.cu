@@ -158,11 +158,15 @@ __global__ void fix_absmax_kernel(const long long *buf, int nx, long long rows, 
                                   unsigned long long *out)
 {
     unsigned long long m = 0;
-    const long long n = (long long)nx * rows;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long r = i / nx;
-        const long long v = buf[r * pitch + (i - r * nx)];
-        m = max(m, (unsigned long long)(v < 0 ? -v : v));
+    // warps take whole rows (no division per cell), lanes walk a row
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long r = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+        const long long *row = buf + r * pitch;
+        for (int x = lane; x < nx; x += 32) {
+            const long long v = row[x];
+            m = max(m, (unsigned long long)(v < 0 ? -v : v));
+        }
     }
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
