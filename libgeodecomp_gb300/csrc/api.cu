@@ -76,23 +76,26 @@ int fix_scale_exp(const Grid& g)
 }
 
 // dense (x-fastest, rows of nx) doubles -> pitched fixed point
+// (warps take whole rows, lanes walk a row: no division per cell)
 __global__ void to_fix_pitched_kernel(const double *src, long long *dst, int nx, long long rows, long long pitch, int exp)
 {
-    const long long n = (long long)nx * rows;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long r = i / nx;
-        const long long x = i - r * nx;
-        dst[r * pitch + x] = __double2ll_rn(ldexp(src[i], LGD_FIX_BITS - exp));
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long r = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+        for (int x = lane; x < nx; x += 32) {
+            dst[r * pitch + x] = __double2ll_rn(ldexp(src[r * nx + x], LGD_FIX_BITS - exp));
+        }
     }
 }
 
 __global__ void from_fix_pitched_kernel(const long long *src, double *dst, int nx, long long rows, long long pitch, int exp)
 {
-    const long long n = (long long)nx * rows;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long r = i / nx;
-        const long long x = i - r * nx;
-        dst[i] = ldexp((double)src[r * pitch + x], exp - LGD_FIX_BITS);
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long r = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+        for (int x = lane; x < nx; x += 32) {
+            dst[r * nx + x] = ldexp((double)src[r * pitch + x], exp - LGD_FIX_BITS);
+        }
     }
 }
 
