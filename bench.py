@@ -1001,6 +1001,8 @@ def run_surrogate(args):
     # the same run with a judge that accepts the network's own error level:
     # what the surrogate path costs and how far it drifts when it is used
     u_rel, t_rel, st_rel = S.run_surrogate_with_judge(params, u0, kap, steps, tol=args.relaxed_tol)
+    # and with the judge at the accuracy bar itself (one call within 1e-3)
+    u_bar, t_bar, st_bar = S.run_surrogate_with_judge(params, u0, kap, steps, tol=1e-3)
     net_ms = S.time_calls(params, u0, kap, calls=8)
     line = {
         "metric": "surrogate vs plain time at rel-L2<=1e-3", "value": round(t_plain / t_sur, 4),
@@ -1021,6 +1023,9 @@ def run_surrogate(args):
         "relaxed_judge": {"tol": args.relaxed_tol, "surrogate_judge_s": round(t_rel, 4),
                           "plain_over_surrogate": round(t_plain / t_rel, 4), "fallbacks": st_rel["fallbacks"],
                           "segments": st_rel["segments"], "rel_l2_vs_fp64": S.rel_l2(u_rel, u64)},
+        "judge_at_1e-3": {"tol": 1e-3, "surrogate_judge_s": round(t_bar, 4),
+                          "plain_over_surrogate": round(t_plain / t_bar, 4), "fallbacks": st_bar["fallbacks"],
+                          "segments": st_bar["segments"], "rel_l2_vs_fp64": S.rel_l2(u_bar, u64)},
         "net_call_ms": round(net_ms, 4),
         "net_call_tflops": round(S.FLOP_PER_VOXEL * n ** 3 / (net_ms * 1e-3) / 1e12, 1),
         "plain_16_steps_ms": round(t_plain / steps * S.STEPS_PER_CALL * 1e3, 4),
