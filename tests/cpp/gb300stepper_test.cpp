@@ -266,6 +266,36 @@ static void compareSlabs(Coord<APITraits::SelectTopology<CELL>::Value::DIM> dim,
     }
 }
 
+// arguments the stepper refuses, each with std::invalid_argument and no
+// leaked initializer (the stepper owns and deletes it either way)
+static void testStepperErrors()
+{
+    struct Case {
+        int rank, ranks;
+        unsigned ghost;
+        bool link;
+    };
+    const Case cases[] = {
+        {2, 2, 4, false},     // rank outside the world
+        {0, 0, 4, false},     // no ranks
+        {0, 2, 4, false},     // several ranks without a link
+        {0, 2, 0, true},      // ghost width zero
+        {0, 3, 16, true},     // 30 planes over 3 ranks: fewer planes than the ghost width
+    };
+    Hub hub(3);
+    for (const Case& c : cases) {
+        ThreadLink link(&hub, 0);
+        bool threw = false;
+        try {
+            GB300SlabStepper<JacobiCell> st(new ValueInit<JacobiCell>(Coord<3>(8, 8, 30), 4), c.rank, c.ranks, c.ghost,
+                                            c.link ? &link : 0);
+        } catch (const std::invalid_argument&) {
+            threw = true;
+        }
+        EXPECT(threw);
+    }
+}
+
 int main()
 {
     int n = 0;
@@ -278,6 +308,7 @@ int main()
     compareSlabs<LifeCell>(Coord<2>(70, 41), 2, 6, 31, false);
     compareSlabs<LifeCell>(Coord<2>(64, 60), 4, 5, 23, false);
     compareSlabs<AverageCell>(Coord<3>(20, 16, 24), 3, 3, 14, false);
+    testStepperErrors();
     if (failures) {
         std::printf("%d failure(s)\n", failures);
         return 1;

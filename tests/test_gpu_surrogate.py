@@ -6,6 +6,8 @@ the plain stencil when the network is wrong."""
 import numpy as np
 import pytest
 
+from libgeodecomp_gb300 import lgd
+
 from oracle import surrogate_ref as sr
 
 pytestmark = pytest.mark.gpu
@@ -157,6 +159,9 @@ def test_data_parallel_training_follows_the_global_batch():
     np.testing.assert_allclose(pa, single, rtol=1e-3, atol=1e-5)
     np.testing.assert_allclose(ha, hist1, rtol=1e-3)
     assert not np.array_equal(pa, p0)
+    with S.SurrogateNet((32, 32, 32), batch=1, channels=24) as net:      # no training buffers
+        with pytest.raises(lgd.LGDError):
+            net.set_grads(np.zeros(net.P, dtype=np.float32))
 
 
 def test_judge_falls_back_to_the_plain_stencil():
