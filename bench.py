@@ -969,7 +969,7 @@ def run_surrogate(args):
     n = args.surrogate_size
     steps = args.surrogate_steps
     t0 = time.perf_counter()
-    states, kappa_tr = S.make_trajectories(count=args.trajectories, n=32, calls=4, length=16.0, seed=7)
+    states, kappa_tr = S.make_trajectories(count=args.trajectories, n=args.train_size, calls=4, length=16.0, seed=7)
     t_data = time.perf_counter() - t0
     t0 = time.perf_counter()
     params, hist = S.train(states, kappa_tr, channels=24, iters=args.train_iters, batch=8, lr=1e-3, seed=1)
@@ -1012,14 +1012,17 @@ def run_surrogate(args):
         "config": {"workload": "surrogate_varcoef_%d" % n, "grid": [n, n, n], "t_final": steps,
                    "kappa": "GRF length 16 mapped to [0.02, 0.15]", "net": "4 x conv3^3, 24 ch, GELU, residual",
                    "steps_per_call": S.STEPS_PER_CALL, "judge_every_calls": S.CALLS_PER_JUDGE,
-                   "judge_tol": args.judge_tol, "trajectories": args.trajectories, "train_iters": args.train_iters},
+                   "judge_tol": args.judge_tol, "trajectories": args.trajectories, "train_iters": args.train_iters,
+                   "train_size": args.train_size},
         "plain_fp32_s": round(t_plain, 4), "plain_fp64_s": round(t_fp64, 4), "surrogate_judge_s": round(t_sur, 4),
         "comparators": {"fp64_over_surrogate": round(t_fp64 / t_sur, 4),
                         "fp64_over_relaxed_surrogate": round(t_fp64 / t_rel, 4),
                         "fp32_over_surrogate": round(t_plain / t_sur, 4)},
         "rel_l2_vs_fp64": {"plain_fp32": S.rel_l2(u_plain, u64), "surrogate_judge": S.rel_l2(u_sur, u64)},
         "judge": {"segments": stats["segments"], "fallbacks": stats["fallbacks"],
-                  "max_error": max(stats["judge_errors"]) if stats["judge_errors"] else None},
+                  "max_error": max(stats["judge_errors"]) if stats["judge_errors"] else None,
+                  "min_error": min(stats["judge_errors"]) if stats["judge_errors"] else None,
+                  "median_error": float(np.median(stats["judge_errors"])) if stats["judge_errors"] else None},
         "relaxed_judge": {"tol": args.relaxed_tol, "surrogate_judge_s": round(t_rel, 4),
                           "plain_over_surrogate": round(t_plain / t_rel, 4), "fallbacks": st_rel["fallbacks"],
                           "segments": st_rel["segments"], "rel_l2_vs_fp64": S.rel_l2(u_rel, u64)},
@@ -1082,6 +1085,7 @@ def main():
     ap.add_argument("--surrogate-steps", type=int, default=4096)
     ap.add_argument("--trajectories", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=6000)
+    ap.add_argument("--train-size", type=int, default=32, help="edge of the training trajectories' tori")
     ap.add_argument("--judge-tol", type=float, default=1e-4)
     ap.add_argument("--relaxed-tol", type=float, default=1e-2)
     ap.add_argument("--net-calls", type=int, default=0, help="time this many surrogate network calls alone")
