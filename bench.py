@@ -996,6 +996,7 @@ def run_surrogate(args):
     finally:
         ref.close()
     S.run_plain(u0, kap, 16)                         # warm-up
+    S.run_surrogate_with_judge(params, u0, kap, S.STEPS_PER_CALL * S.CALLS_PER_JUDGE, tol=args.judge_tol)
     u_plain, t_plain = S.run_plain(u0, kap, steps)
     u_sur, t_sur, stats = S.run_surrogate_with_judge(params, u0, kap, steps, tol=args.judge_tol)
     # the same run with a judge that accepts the network's own error level:
@@ -1085,7 +1086,7 @@ def main():
     ap.add_argument("--surrogate-steps", type=int, default=4096)
     ap.add_argument("--trajectories", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=6000)
-    ap.add_argument("--train-size", type=int, default=32, help="edge of the training trajectories' tori")
+    ap.add_argument("--train-size", type=int, default=64, help="edge of the training trajectories' tori")
     ap.add_argument("--judge-tol", type=float, default=1e-4)
     ap.add_argument("--relaxed-tol", type=float, default=1e-2)
     ap.add_argument("--net-calls", type=int, default=0, help="time this many surrogate network calls alone")
