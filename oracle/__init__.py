@@ -26,12 +26,13 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile the C restatement (gcc, OpenMP, no FMA contraction)."""
+    """Compile the C restatement (gcc -O3, OpenMP, no FMA contraction: the
+    vectorised loops keep every cell's operations and their order)."""
     src = os.path.join(HERE, "lgd_oracle.c")
     hdr = os.path.join(HERE, "lbm_d3q19.h")
     newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
-        cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+        cmd = ["gcc", "-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
                src, "-o", LIB_PATH + ".tmp"]
         subprocess.check_call(cmd)
         os.replace(LIB_PATH + ".tmp", LIB_PATH)

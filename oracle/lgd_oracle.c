@@ -59,6 +59,25 @@ static inline long wrap(long i, long n)
  * (storage/soagrid.h:578-585), Torus wraps (geometry/topologies.h:179-253).
  * new = (c + n + s + e + w + t + b) * (1/7) with n = y-1, s = y+1, e = x+1,
  * w = x-1, t = z+1, b = z-1, summed left to right. */
+/* One row of a cube grid whose y and z neighbours all lie inside: the x
+ * loop between the row's ends reads no edge value, so the compiler can
+ * vectorise it (each lane the same additions in the same order, so the
+ * results do not change); the reference's updateLineX vectorises the same
+ * loop with libflatarray's short_vec. */
+static void jacobi7_inner_row(long nx, double edge, const double *c, const double *n, const double *s,
+                              const double *t, const double *b, double *d)
+{
+    if (nx == 1) {
+        d[0] = (c[0] + n[0] + s[0] + edge + edge + t[0] + b[0]) * (1.0 / 7.0);
+        return;
+    }
+    d[0] = (c[0] + n[0] + s[0] + c[1] + edge + t[0] + b[0]) * (1.0 / 7.0);
+    for (long x = 1; x < nx - 1; ++x) {
+        d[x] = (c[x] + n[x] + s[x] + c[x + 1] + c[x - 1] + t[x] + b[x]) * (1.0 / 7.0);
+    }
+    d[nx - 1] = (c[nx - 1] + n[nx - 1] + s[nx - 1] + edge + c[nx - 2] + t[nx - 1] + b[nx - 1]) * (1.0 / 7.0);
+}
+
 static void jacobi7_step(long nx, long ny, long nz, int torus, double edge,
                          const double *src, double *dst)
 {
@@ -66,6 +85,11 @@ static void jacobi7_step(long nx, long ny, long nz, int torus, double edge,
 #pragma omp parallel for schedule(static)
     for (z = 0; z < nz; ++z) {
         for (long y = 0; y < ny; ++y) {
+            if (!torus && y > 0 && y < ny - 1 && z > 0 && z < nz - 1) {
+                const double *c = src + (z * ny + y) * nx;
+                jacobi7_inner_row(nx, edge, c, c - nx, c + nx, c + ny * nx, c - ny * nx, dst + (z * ny + y) * nx);
+                continue;
+            }
             for (long x = 0; x < nx; ++x) {
                 double c = src[(z * ny + y) * nx + x];
                 double n, s, e, w, t, b;
