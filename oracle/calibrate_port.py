@@ -7,7 +7,7 @@ where oracle/_ref/lgd_ref is built from the reference's own headers
 (oracle/Makefile), so that the port's figure can be read as the reference's:
 a ratio port/reference below 1 means the port is slower than the reference.
 
-    python oracle/calibrate_port.py [--threads T] [--only jacobi,gol,sell]
+    python oracle/calibrate_port.py [--threads T] [--only jacobi,gol,sell,lbm]
 
 Prints one JSON object per workload.  Test infrastructure: nothing of the
 library runs here.
@@ -88,16 +88,25 @@ def sell(tmp, threads, n=1 << 20, steps=10):
             "port_glups": n * steps / port_s / 1e9, "port_over_ref": ref_step * steps / port_s}
 
 
+def lbm(tmp, threads, edge=96, steps=10, omega=1.7):
+    ref_s = min(run_ref(["lbm", edge, steps, omega, 0.05, os.path.join(tmp, "o.f64"), "omp", "time"],
+                        threads)["seconds"] for _ in range(3))
+    port_s = best_of(lambda: oracle.lbm(edge, steps, omega, 0.05, threads=threads))
+    cells = edge ** 3 * steps
+    return {"workload": "d3q19 %d^3 x %d" % (edge, steps), "ref_glups": cells / ref_s / 1e9,
+            "port_glups": cells / port_s / 1e9, "port_over_ref": ref_s / port_s}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--threads", type=int, default=8)
-    ap.add_argument("--only", default="jacobi,gol,sell")
+    ap.add_argument("--only", default="jacobi,gol,sell,lbm")
     args = ap.parse_args()
     if not os.path.exists(os.path.join(HERE, "_ref", "lgd_ref")):
         sys.exit("oracle/_ref/lgd_ref is not built (make -C oracle)")
     with tempfile.TemporaryDirectory() as tmp:
         for name in args.only.split(","):
-            r = {"jacobi": jacobi, "gol": gol, "sell": sell}[name](tmp, args.threads)
+            r = {"jacobi": jacobi, "gol": gol, "sell": sell, "lbm": lbm}[name](tmp, args.threads)
             r.update(threads=args.threads)
             print(json.dumps({k: round(v, 4) if isinstance(v, float) else v for k, v in r.items()}), flush=True)
 

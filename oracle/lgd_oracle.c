@@ -362,6 +362,58 @@ int lgd_oracle_sell_diffusion(int n, int C, const int *chunk_offset, const int *
  * Reference: the D3Q19 cell in oracle/ref_driver.cpp (collision of
  * src/examples/latticeboltzmann/main.cpp:93-170), on an L^3 fluid box with
  * walls outside and the lid beyond y = L-1.  f is SoA: f[i * L^3 + idx]. */
+
+/* one cell next to a wall: populations from outside bounce back */
+static void lbm_cell_wall(const double *a, double *b, size_t cells, long L, long x, long y, long z, double omega,
+                          double lid)
+{
+    const size_t idx = ((size_t)z * L + y) * L + x;
+    double self[19];
+    double pulled[19];
+    double out[19];
+    for (int i = 0; i < 19; ++i) {
+        self[i] = a[i * cells + idx];
+    }
+    for (int i = 0; i < 19; ++i) {
+        long sx = x - LGD_D3Q19_E[i][0];
+        long sy = y - LGD_D3Q19_E[i][1];
+        long sz = z - LGD_D3Q19_E[i][2];
+        if (sx >= 0 && sx < L && sy >= 0 && sy < L && sz >= 0 && sz < L) {
+            pulled[i] = a[i * cells + ((size_t)sz * L + sy) * L + sx];
+        } else {
+            int fromLid = (y == L - 1) && (LGD_D3Q19_E[i][1] == -1);
+            pulled[i] = lgd_d3q19_bounce(self, i, fromLid ? lid : 0.0);
+        }
+    }
+    lgd_d3q19_collide(pulled, omega, out);
+    for (int i = 0; i < 19; ++i) {
+        b[i * cells + idx] = out[i];
+    }
+}
+
+/* cells x0 .. x1-1 of a row whose every neighbour lies inside the box: the
+ * same pulls without the wall tests, the same collision (the compiler may
+ * vectorise the row; each cell's operations and their order are unchanged,
+ * as in the reference's vectorised updateLineX) */
+static void lbm_row_inner(const double *restrict a, double *restrict b, size_t cells, long L, long y, long z,
+                          long x0, long x1, double omega)
+{
+    const size_t row = ((size_t)z * L + y) * L;
+    for (long x = x0; x < x1; ++x) {
+        const size_t idx = row + x;
+        double pulled[19];
+        double out[19];
+        for (int i = 0; i < 19; ++i) {
+            const long off = LGD_D3Q19_E[i][0] + LGD_D3Q19_E[i][1] * L + LGD_D3Q19_E[i][2] * L * L;
+            pulled[i] = a[i * cells + idx - off];
+        }
+        lgd_d3q19_collide(pulled, omega, out);
+        for (int i = 0; i < 19; ++i) {
+            b[i * cells + idx] = out[i];
+        }
+    }
+}
+
 int lgd_oracle_lbm(int L, int steps, double omega, double lid, double *f, int threads)
 {
     size_t cells = (size_t)L * L * L;
@@ -377,29 +429,12 @@ int lgd_oracle_lbm(int L, int steps, double omega, double lid, double *f, int th
 #pragma omp parallel for schedule(static)
         for (z = 0; z < L; ++z) {
             for (long y = 0; y < L; ++y) {
-                for (long x = 0; x < L; ++x) {
-                    size_t idx = ((size_t)z * L + y) * L + x;
-                    double self[19];
-                    double pulled[19];
-                    double out[19];
-                    for (int i = 0; i < 19; ++i) {
-                        self[i] = a[i * cells + idx];
-                    }
-                    for (int i = 0; i < 19; ++i) {
-                        long sx = x - LGD_D3Q19_E[i][0];
-                        long sy = y - LGD_D3Q19_E[i][1];
-                        long sz = z - LGD_D3Q19_E[i][2];
-                        if (sx >= 0 && sx < L && sy >= 0 && sy < L && sz >= 0 && sz < L) {
-                            pulled[i] = a[i * cells + ((size_t)sz * L + sy) * L + sx];
-                        } else {
-                            int fromLid = (y == L - 1) && (LGD_D3Q19_E[i][1] == -1);
-                            pulled[i] = lgd_d3q19_bounce(self, i, fromLid ? lid : 0.0);
-                        }
-                    }
-                    lgd_d3q19_collide(pulled, omega, out);
-                    for (int i = 0; i < 19; ++i) {
-                        b[i * cells + idx] = out[i];
-                    }
+                if (L >= 3 && z >= 1 && z <= L - 2 && y >= 1 && y <= L - 2) {
+                    lbm_cell_wall(a, b, cells, L, 0, y, z, omega, lid);
+                    lbm_row_inner(a, b, cells, L, y, z, 1, L - 1, omega);
+                    lbm_cell_wall(a, b, cells, L, L - 1, y, z, omega, lid);
+                } else {
+                    for (long x = 0; x < L; ++x) lbm_cell_wall(a, b, cells, L, x, y, z, omega, lid);
                 }
             }
         }
