@@ -1102,7 +1102,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
-    world, rank, local, dist = dist_setup("nccl" if world > 1 and slab_capable(args.workload) else "gloo")
+    # NCCL where the ranks exchange device data (slabs, SELL row blocks)
+    exchanges = slab_capable(args.workload) or args.workload == "sell_f64_4m"
+    world, rank, local, dist = dist_setup("nccl" if world > 1 and exchanges else "gloo")
     run_gpu(args, world, rank, local, dist)
 
 
