@@ -94,14 +94,16 @@ class TorchComm:
         self.rank = dist.get_rank()
 
     def exchange(self, sends, recvs):
-        """sends: [(peer, tensor)], recvs: [(peer, tensor)]; all posted
-        before any wait, so pairs of ranks cannot deadlock."""
-        reqs = []
-        for peer, t in recvs:
-            reqs.append(self.dist.irecv(t, src=peer))
-        for peer, t in sends:
-            reqs.append(self.dist.isend(t, dst=peer))
-        for r in reqs:
+        """sends: [(peer, tensor)], recvs: [(peer, tensor)], posted as one
+        batch: with NCCL the operations of a batch run as one group, so a
+        receive queued ahead of a send cannot block it (pairs of ranks that
+        each receive first would deadlock otherwise), and operations to the
+        same peer are matched in the order they were posted."""
+        ops = [self.dist.P2POp(self.dist.irecv, t, peer) for peer, t in recvs]
+        ops += [self.dist.P2POp(self.dist.isend, t, peer) for peer, t in sends]
+        if not ops:
+            return
+        for r in self.dist.batch_isend_irecv(ops):
             r.wait()
 
     def allgather(self, send, recvs):
