@@ -632,6 +632,54 @@ def measure(torch, w, steps, warmup, local, dist, world, peak, peak_kind):
             "roofline": roofline_of(w, ms, steps, launches, peak, peak_kind)}
 
 
+def sell_renumbering(torch, w, steps=50):
+    """ms per step of the SELL kernel with and without the reverse
+    Cuthill-McKee numbering (LGD_SELL_RENUMBER; every node's value is
+    bit-identical either way): the configuration's graph, whose targets are
+    uniform at random, and a periodic 160^3 7-point mesh numbered at random,
+    whose locality the numbering recovers."""
+    from libgeodecomp_gb300 import lgd, workloads
+
+    def timed(g):
+        st = torch.cuda.ExternalStream(g.stream())
+        g.step(3)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        g.step(steps)
+        b.record(st)
+        b.synchronize()
+        return a.elapsed_time(b) / steps
+
+    out = {}
+    rp, col, wt = workloads.powerlaw_graph(w.n, seed=42)
+    with lgd.SellGrid.from_csr(w.n, rp, col, wt, 32, 256, renumber=True) as g:
+        g.upload(w.x0)
+        out["config_graph_ms_per_step"] = {"plain": round(timed(w.g), 4), "renumbered": round(timed(g), 4)}
+    del rp, col, wt
+    n1 = 160
+    n = n1 ** 3
+    idx = np.arange(n, dtype=np.int64).reshape(n1, n1, n1)
+    perm = np.random.default_rng(7).permutation(n)
+    rows = np.concatenate([perm[idx.ravel()]] * 6)
+    cols = np.concatenate([perm[np.roll(idx, shift=d, axis=(0, 1, 2)).ravel()]
+                           for d in ((0, 0, 1), (0, 0, -1), (0, 1, 0), (0, -1, 0), (1, 0, 0), (-1, 0, 0))])
+    o = np.argsort(rows, kind="stable")
+    cols = cols[o].astype(np.int32)
+    rpm = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rpm, rows + 1, 1)
+    rpm = np.cumsum(rpm)
+    wm = np.full(cols.size, 0.15)
+    x0 = workloads.sell_values(n, seed=3)
+    mesh = {}
+    for renumber in (False, True):
+        with lgd.SellGrid.from_csr(n, rpm, cols, wm, 32, 256, renumber=renumber) as g:
+            g.upload(x0)
+            mesh["renumbered" if renumber else "random_numbering"] = round(timed(g), 4)
+    out["mesh_160cubed_ms_per_step"] = mesh
+    return out
+
+
 def run_secondary(torch, args, local, peak, peak_kind):
     """The other configurations, one compact block each."""
     out = {}
@@ -646,6 +694,7 @@ def run_secondary(torch, args, local, peak, peak_kind):
                      "clocks": m["clocks"], "setup": w.setup}
             if name == "sell_f64_4m":
                 block["s_per_step"] = round(m["ms"] / steps * 1e-3, 7)
+                block["renumbering"] = sell_renumbering(torch, w)
             if name == "lbm_d3q19_ensemble_512":
                 lms = w.looped_ms(torch, 4)
                 block["looped_single_grid_launches"] = {"ms_per_step": round(lms, 3),

@@ -45,6 +45,25 @@ typedef struct lgd_sell lgd_sell;
 /* flags */
 #define LGD_SELL_EXACT 1   /* separate multiply and add (bit-identical to the
                               reference build); default fuses them (FMA) */
+#define LGD_SELL_RENUMBER 2 /* lgd_sell_create_from_csr (host input): number
+                              the nodes in reverse Cuthill-McKee order before
+                              the build, so that rows near each other read
+                              columns near each other; logical order at the
+                              boundary stays the caller's (the permutation
+                              composes both numberings).  The container
+                              orders a row's entries by physical column, as
+                              the reference's does, so the renumbered grid
+                              adds each row's terms in another order: its
+                              values agree with the plain grid's to
+                              rounding, not bit for bit, and its arrays
+                              differ from the reference's container. */
+
+/* Reverse Cuthill-McKee order of a graph (CSR row_ptr[n+1], col
+ * [row_ptr[n]], edges taken in both directions): order[k] = the node that
+ * gets number k.  Each connected part starts from a node of least degree;
+ * neighbours join the breadth-first sweep by increasing degree.  Host code,
+ * no GPU needed. */
+int lgd_graph_rcm(int n, const int64_t *row_ptr, const int32_t *col, int32_t *order);
 
 /* Uploads the SELL arrays (chunk_offset[n_chunks+1], row_length
  * [rows_padded], values/column[total] with physical column ids) and

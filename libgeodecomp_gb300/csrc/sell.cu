@@ -635,9 +635,141 @@ int lgd_sell_create(int n, int C, int64_t total, const int32_t *chunk_offset, co
     });
 }
 
+namespace {
+
+// order[k] = the node numbered k: reverse Cuthill-McKee over the graph's
+// edges in both directions
+std::vector<int32_t> rcm_order(int n, const int64_t *rp, const int32_t *col)
+{
+    const int64_t nnz = rp[n];
+    std::vector<int64_t> deg(n, 0);
+    std::vector<int64_t> trp((size_t)n + 1, 0);
+    for (int r = 0; r < n; ++r) {
+        deg[r] += rp[r + 1] - rp[r];
+        for (int64_t e = rp[r]; e < rp[r + 1]; ++e) {
+            const int32_t c = col[e];
+            if (c < 0 || c >= n) throw Error(LGD_ERR_RANGE, "column id outside the node set");
+            ++trp[(size_t)c + 1];
+            ++deg[c];
+        }
+    }
+    for (int r = 0; r < n; ++r) trp[(size_t)r + 1] += trp[r];
+    std::vector<int32_t> tcol((size_t)nnz);
+    {
+        std::vector<int64_t> fill(trp.begin(), trp.end() - 1);
+        for (int r = 0; r < n; ++r) {
+            for (int64_t e = rp[r]; e < rp[r + 1]; ++e) tcol[(size_t)fill[col[e]]++] = r;
+        }
+    }
+    std::vector<int32_t> by_degree(n);
+    for (int i = 0; i < n; ++i) by_degree[i] = i;
+    std::stable_sort(by_degree.begin(), by_degree.end(), [&](int32_t a, int32_t b) { return deg[a] < deg[b]; });
+    std::vector<char> seen(n, 0);
+    std::vector<int32_t> order;
+    order.reserve(n);
+    std::vector<int32_t> nb;
+    size_t head = 0;
+    for (int32_t start : by_degree) {
+        if (seen[start]) continue;
+        seen[start] = 1;
+        order.push_back(start);
+        for (; head < order.size(); ++head) {
+            const int32_t u = order[head];
+            nb.clear();
+            for (int64_t e = rp[u]; e < rp[u + 1]; ++e) {
+                if (!seen[col[e]]) {
+                    seen[col[e]] = 1;
+                    nb.push_back(col[e]);
+                }
+            }
+            for (int64_t e = trp[u]; e < trp[(size_t)u + 1]; ++e) {
+                if (!seen[tcol[e]]) {
+                    seen[tcol[e]] = 1;
+                    nb.push_back(tcol[e]);
+                }
+            }
+            std::stable_sort(nb.begin(), nb.end(), [&](int32_t a, int32_t b) { return deg[a] < deg[b]; });
+            order.insert(order.end(), nb.begin(), nb.end());
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+__global__ void compose_perm_kernel(int *perm, const int32_t *order, int n)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) perm[p] = order[perm[p]];
+}
+
+}  // namespace
+
+int lgd_graph_rcm(int n, const int64_t *row_ptr, const int32_t *col, int32_t *order)
+{
+    return guard([&] {
+        LGD_REQUIRE(n > 0 && row_ptr != nullptr && order != nullptr, LGD_ERR_INVALID, "empty graph or null array");
+        LGD_REQUIRE(row_ptr[n] == 0 || col != nullptr, LGD_ERR_INVALID, "null column array");
+        const std::vector<int32_t> o = rcm_order(n, row_ptr, col);
+        std::copy(o.begin(), o.end(), order);
+    });
+}
+
 int lgd_sell_create_from_csr(int n, const int64_t *row_ptr, const int32_t *col, const double *w, int C, int sigma,
                              int device_input, int precision, int flags, lgd_sell **out)
 {
+    if (flags & LGD_SELL_RENUMBER) {
+        // number the nodes in reverse Cuthill-McKee order, build from the
+        // renumbered CSR, then compose the permutation so that logical
+        // order stays the caller's
+        return guard([&] {
+            LGD_REQUIRE(out != nullptr, LGD_ERR_INVALID, "null output");
+            *out = nullptr;
+            LGD_REQUIRE(!device_input, LGD_ERR_UNSUPPORTED, "renumbering takes the CSR arrays in host memory");
+            LGD_REQUIRE(n > 0 && row_ptr != nullptr, LGD_ERR_INVALID, "node count must be positive");
+            const int64_t nnz = row_ptr[n];
+            LGD_REQUIRE(nnz == 0 || (col && w), LGD_ERR_INVALID, "null matrix arrays");
+            const std::vector<int32_t> order = rcm_order(n, row_ptr, col);
+            std::vector<int32_t> inv(n);
+            for (int k = 0; k < n; ++k) inv[order[k]] = k;
+            std::vector<int64_t> rp2((size_t)n + 1, 0);
+            std::vector<int32_t> col2((size_t)nnz);
+            std::vector<double> w2((size_t)nnz);
+            for (int k = 0; k < n; ++k) {
+                const int r = order[k];
+                int64_t o = rp2[k];
+                for (int64_t e = row_ptr[r]; e < row_ptr[r + 1]; ++e, ++o) {
+                    col2[(size_t)o] = inv[col[e]];
+                    w2[(size_t)o] = w[e];
+                }
+                rp2[(size_t)k + 1] = o;
+            }
+            lgd_sell *h = nullptr;
+            const int rc = lgd_sell_create_from_csr(n, rp2.data(), col2.data(), w2.data(), C, sigma, 0, precision,
+                                                    flags & ~LGD_SELL_RENUMBER, &h);
+            if (rc != LGD_OK) {
+                char msg[512];
+                lgd_gpu_last_error(msg, sizeof(msg));
+                throw Error(rc, std::string("renumbered matrix: ") + msg);
+            }
+            Sell& s = sell_of(h);
+            int32_t *d_order = nullptr;
+            try {
+                LGD_CHECK_CUDA(cudaMalloc(&d_order, sizeof(int32_t) * (size_t)n));
+                LGD_CHECK_CUDA(cudaMemcpyAsync(d_order, order.data(), sizeof(int32_t) * (size_t)n,
+                                               cudaMemcpyHostToDevice, s.stream));
+                compose_perm_kernel<<<(unsigned)std::min(152 * 16, (n + 255) / 256), 256, 0, s.stream>>>(s.d_perm, d_order,
+                                                                                                         n);
+                check_launch("sell renumbering");
+                LGD_CHECK_CUDA(cudaStreamSynchronize(s.stream));
+            } catch (...) {
+                cudaFree(d_order);
+                lgd_sell_destroy(h);
+                throw;
+            }
+            cudaFree(d_order);
+            s.flags = flags;
+            *out = h;
+        });
+    }
     return guard([&] {
         using namespace sbuild;
         LGD_REQUIRE(out != nullptr, LGD_ERR_INVALID, "null output");

@@ -131,6 +131,7 @@ def lib():
             "lgd_sell_update_rows": [P, I, I],
             "lgd_sell_swap": [P],
             "lgd_sell_x_device": [P, I, P, P],
+            "lgd_graph_rcm": [I, P, P, P],
             "lgd_sell_synchronize": [P],
             "lgd_sell_stream": [P, P],
             "lgd_sell_launch_count": [P, P],
@@ -349,6 +350,7 @@ class Grid:
 
 # ----------------------------------------------------------- SELL-C-sigma
 SELL_EXACT = 1
+SELL_RENUMBER = 2
 
 
 def snapshot_info(path: str, dim: int = 3):
@@ -388,15 +390,28 @@ SELL_GPU_MAX_SIGMA = 4096     # LGD_SELL_GPU_MAX_SIGMA
 SELL_GPU_MAX_ROW = 1024       # LGD_SELL_GPU_MAX_ROW
 
 
+def graph_rcm(n: int, row_ptr, col) -> np.ndarray:
+    """Reverse Cuthill-McKee order of a CSR graph (lgd_graph_rcm, host
+    code): order[k] = the node numbered k."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cc = np.ascontiguousarray(col, dtype=np.int32)
+    out = np.empty(n, dtype=np.int32)
+    check(lib().lgd_graph_rcm(n, _ptr(rp), _ptr(cc) if cc.size else None, _ptr(out)))
+    return out
+
+
 class SellGrid:
     """Device SELL-C-sigma grid running the diffusion cell."""
 
     @classmethod
     def from_csr(cls, n: int, row_ptr, col, w, C: int, sigma: int, precision: int = 8, exact: bool = False,
-                 device: bool = False):
+                 device: bool = False, renumber: bool = False):
         """Builds the matrix on the GPU (lgd_sell_create_from_csr).  With
         device=True the CSR arrays are torch CUDA tensors (int64, int32,
-        float64), else numpy arrays."""
+        float64), else numpy arrays.  renumber=True numbers the nodes in
+        reverse Cuthill-McKee order first (host arrays; logical order
+        unchanged; each row's terms are added in another order, so values
+        agree with the plain grid's to rounding)."""
         self = cls.__new__(cls)
         self.n = n
         if device:
@@ -408,8 +423,9 @@ class SellGrid:
             ptrs = [_ptr(a) if a.size else ctypes.c_void_p() for a in self._keep]
         self._h = ctypes.c_void_p()
         self._C = C
+        flags = (SELL_EXACT if exact else 0) | (SELL_RENUMBER if renumber else 0)
         check(lib().lgd_sell_create_from_csr(n, ptrs[0], ptrs[1], ptrs[2], C, sigma, int(device), precision,
-                                             SELL_EXACT if exact else 0, ctypes.byref(self._h)))
+                                             flags, ctypes.byref(self._h)))
         return self
 
     def layout(self) -> dict:

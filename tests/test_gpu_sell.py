@@ -186,3 +186,39 @@ def test_sell_rejects_bad_arguments():
         with pytest.raises(lgd.LGDError) as e:
             lgd.check(lgd.lib().lgd_sell_upload_x(g._h, 0, 1, lgd._ptr(a), a.nbytes))
         assert e.value.code == lgd.ERR_INVALID
+
+
+# ------------------------------------------------ reverse Cuthill-McKee
+@pytest.mark.parametrize("exact,precision", [(True, 8), (False, 8), (False, 4)])
+def test_renumbered_grid_agrees_to_rounding(exact, precision):
+    """LGD_SELL_RENUMBER builds the matrix on RCM node numbers.  The
+    container orders a row's entries by physical column (the reference's
+    layout), so the renumbered grid adds each row's terms in another order:
+    every node's value (in the caller's logical order) agrees with the plain
+    grid's to a few units in the last place - on the power-law graph and on
+    a randomly numbered periodic 3D mesh."""
+    from test_graph_rcm import permuted_mesh
+    n1 = 36
+    n_mesh, rp_mesh, col_mesh = permuted_mesh(n1, seed=8)
+    w_mesh = np.random.default_rng(9).random(col_mesh.size) * (0.9 / 6.0)
+    n_pl = 60013
+    rp_pl, col_pl, w_pl = workloads.powerlaw_graph(n_pl, seed=13)
+    for n, rp, col, w in ((n_pl, rp_pl, col_pl, w_pl), (n_mesh, rp_mesh, col_mesh, w_mesh)):
+        x0 = workloads.sell_values(n, seed=5)
+        out = []
+        for renumber in (False, True):
+            with lgd.SellGrid.from_csr(n, rp, col, w, 32, 256, precision=precision, exact=exact,
+                                       renumber=renumber) as g:
+                g.upload(x0)
+                g.step(7)
+                out.append(g.download())
+        tol = 1e-12 if precision == 8 else 1e-5
+        assert np.max(np.abs(out[1] - out[0]) / np.abs(out[0])) <= tol
+
+
+def test_renumbering_needs_host_arrays():
+    torch = pytest.importorskip("torch")
+    rp, col, w = workloads.powerlaw_graph(1000, seed=1)
+    t = [torch.as_tensor(a, device="cuda") for a in (rp, col.astype(np.int32), w)]
+    with pytest.raises(lgd.LGDError):
+        lgd.SellGrid.from_csr(1000, t[0], t[1], t[2], 32, 256, device=True, renumber=True)
