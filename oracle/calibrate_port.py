@@ -7,7 +7,7 @@ where oracle/_ref/lgd_ref is built from the reference's own headers
 (oracle/Makefile), so that the port's figure can be read as the reference's:
 a ratio port/reference below 1 means the port is slower than the reference.
 
-    python oracle/calibrate_port.py [--threads T] [--only jacobi,gol,sell,lbm]
+    python oracle/calibrate_port.py [--threads T] [--only jacobi,gol,sell,lbm,varcoef]
 
 Prints one JSON object per workload.  Test infrastructure: nothing of the
 library runs here.
@@ -97,16 +97,29 @@ def lbm(tmp, threads, edge=96, steps=10, omega=1.7):
             "port_glups": cells / port_s / 1e9, "port_over_ref": ref_s / port_s}
 
 
+def varcoef(tmp, threads, edge=128, steps=20):
+    u0, k = workloads.varcoef_fields(edge, seed=42, length=16.0)
+    pu, pk = os.path.join(tmp, "u.f64"), os.path.join(tmp, "k.f64")
+    u0.tofile(pu)
+    k.tofile(pk)
+    ref_s = min(run_ref(["varcoef", edge, edge, edge, steps, pu, pk, os.path.join(tmp, "o.f64"), "omp", "time"],
+                        threads)["seconds"] for _ in range(3))
+    port_s = best_of(lambda: oracle.varcoef(u0, k, steps, threads=threads))
+    cells = u0.size * steps
+    return {"workload": "varcoef %d^3 x %d" % (edge, steps), "ref_glups": cells / ref_s / 1e9,
+            "port_glups": cells / port_s / 1e9, "port_over_ref": ref_s / port_s}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--threads", type=int, default=8)
-    ap.add_argument("--only", default="jacobi,gol,sell,lbm")
+    ap.add_argument("--only", default="jacobi,gol,sell,lbm,varcoef")
     args = ap.parse_args()
     if not os.path.exists(os.path.join(HERE, "_ref", "lgd_ref")):
         sys.exit("oracle/_ref/lgd_ref is not built (make -C oracle)")
     with tempfile.TemporaryDirectory() as tmp:
         for name in args.only.split(","):
-            r = {"jacobi": jacobi, "gol": gol, "sell": sell, "lbm": lbm}[name](tmp, args.threads)
+            r = {"jacobi": jacobi, "gol": gol, "sell": sell, "lbm": lbm, "varcoef": varcoef}[name](tmp, args.threads)
             r.update(threads=args.threads)
             print(json.dumps({k: round(v, 4) if isinstance(v, float) else v for k, v in r.items()}), flush=True)
 
