@@ -86,4 +86,40 @@ static inline void lgd_d3q19_collide(const double *f, double omega, double *out)
     }
 }
 
+/* The same collision for two cells at once (GCC vector extension: each
+ * lane does the scalar function's operations in the same order, so the
+ * results are the scalar ones bit for bit; the compiler maps the pairs to
+ * SIMD registers, as the reference's updateLineX does with short_vec). */
+typedef double lgd_v2d __attribute__((vector_size(16)));
+
+static inline void lgd_d3q19_collide_v2(const lgd_v2d *f, double omega, lgd_v2d *out)
+{
+    lgd_v2d rho = {0.0, 0.0};
+    int i;
+    for (i = 0; i < 19; ++i) {
+        rho += f[i];
+    }
+    const lgd_v2d ux =
+        (f[LGD_Q_E] + f[LGD_Q_NE] + f[LGD_Q_SE] + f[LGD_Q_TE] + f[LGD_Q_BE]) -
+        (f[LGD_Q_W] + f[LGD_Q_NW] + f[LGD_Q_SW] + f[LGD_Q_TW] + f[LGD_Q_BW]);
+    const lgd_v2d uy =
+        (f[LGD_Q_N] + f[LGD_Q_NW] + f[LGD_Q_NE] + f[LGD_Q_TN] + f[LGD_Q_BN]) -
+        (f[LGD_Q_S] + f[LGD_Q_SW] + f[LGD_Q_SE] + f[LGD_Q_TS] + f[LGD_Q_BS]);
+    const lgd_v2d uz =
+        (f[LGD_Q_T] + f[LGD_Q_TW] + f[LGD_Q_TE] + f[LGD_Q_TN] + f[LGD_Q_TS]) -
+        (f[LGD_Q_B] + f[LGD_Q_BW] + f[LGD_Q_BE] + f[LGD_Q_BN] + f[LGD_Q_BS]);
+    const lgd_v2d usq = ux * ux + uy * uy + uz * uz;
+    const lgd_v2d d = rho * (1.0 / 3.0) - 0.5 * usq;
+    const double keep = 1.0 - omega;
+    const double w1 = omega * (1.0 / 6.0);
+    const double w2 = omega * (1.0 / 12.0);
+
+    out[LGD_Q_C] = keep * f[LGD_Q_C] + omega * d;
+    for (i = 1; i < 19; ++i) {
+        const lgd_v2d eu = LGD_D3Q19_E[i][0] * ux + LGD_D3Q19_E[i][1] * uy + LGD_D3Q19_E[i][2] * uz;
+        const double wi = (i < 7) ? w1 : w2;
+        out[i] = keep * f[i] + wi * (d + eu + 1.5 * (eu * eu));
+    }
+}
+
 #endif

@@ -399,7 +399,21 @@ static void lbm_row_inner(const double *restrict a, double *restrict b, size_t c
                           long x0, long x1, double omega)
 {
     const size_t row = ((size_t)z * L + y) * L;
-    for (long x = x0; x < x1; ++x) {
+    long x = x0;
+    for (; x + 1 < x1; x += 2) {            /* two cells at once */
+        const size_t idx = row + x;
+        lgd_v2d pulled[19];
+        lgd_v2d out[19];
+        for (int i = 0; i < 19; ++i) {
+            const long off = LGD_D3Q19_E[i][0] + LGD_D3Q19_E[i][1] * L + LGD_D3Q19_E[i][2] * L * L;
+            memcpy(&pulled[i], a + i * cells + idx - off, sizeof(lgd_v2d));
+        }
+        lgd_d3q19_collide_v2(pulled, omega, out);
+        for (int i = 0; i < 19; ++i) {
+            memcpy(b + i * cells + idx, &out[i], sizeof(lgd_v2d));
+        }
+    }
+    for (; x < x1; ++x) {
         const size_t idx = row + x;
         double pulled[19];
         double out[19];
