@@ -668,7 +668,11 @@ int lgd_gpu_upload(lgd_handle *h, int member, int which, const void *host, size_
             }
             // values well below the exponent's range: lower it (both
             // buffers), then convert the doubles again at the new scale so
-            // that no fraction bit is lost at the boundary
+            // that no fraction bit is lost at the boundary.  An upload whose
+            // maximum needs the current exponent (m in [2^(e-1), 2^e))
+            // keeps it: the buffers' maximum then has its top fraction bit
+            // set, and a scan of both buffers would find nothing to lower.
+            if (m > 0.0 && exp_bound(m) >= g.fix_exp) return;
             const int e_before = g.fix_exp;
             lower_fix_exp(g);
             if (g.fix_exp < e_before) {
