@@ -273,8 +273,8 @@ class JacobiWorkload:
     def host_buffers(self, torch):
         dt = np.float32 if self.f32 else np.float64
         nbytes = self.units * np.dtype(dt).itemsize
-        hin = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(self.shape)
-        hout = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(self.shape)
+        hin = pinned(torch, nbytes).view(dt).reshape(self.shape)
+        hout = pinned(torch, nbytes).view(dt).reshape(self.shape)
         self.g.download(0, out=hin)
         return hin, hout
 
@@ -320,8 +320,8 @@ class GoLWorkload:
         self.g.set_time_block_shape(shape)
 
     def host_buffers(self, torch):
-        hin = torch.empty(self.units, dtype=torch.uint8, pin_memory=True).numpy().reshape(self.shape)
-        hout = torch.empty(self.units, dtype=torch.uint8, pin_memory=True).numpy().reshape(self.shape)
+        hin = pinned(torch, self.units).reshape(self.shape)
+        hout = pinned(torch, self.units).reshape(self.shape)
         self.g.download(0, out=hin)
         return hin, hout
 
@@ -375,8 +375,8 @@ class SellWorkload:
         return self.g.launch_count()
 
     def host_buffers(self, torch):
-        hin = torch.empty(self.n * 8, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64)
-        hout = torch.empty(self.n * 8, dtype=torch.uint8, pin_memory=True).numpy().view(np.float64)
+        hin = pinned(torch, self.n * 8).view(np.float64)
+        hout = pinned(torch, self.n * 8).view(np.float64)
         hin[:] = self.x0
         return hin, hout
 
@@ -422,8 +422,8 @@ class VarcoefWorkload:
         return self.name
 
     def host_buffers(self, torch):
-        hin = torch.empty(self.units * 4, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
-        hout = torch.empty(self.units * 4, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
+        hin = pinned(torch, self.units * 4).view(np.float32)
+        hout = pinned(torch, self.units * 4).view(np.float32)
         hin[:] = self.u0.reshape(-1)
         return hin.reshape(self.shape), hout.reshape(self.shape)
 
@@ -594,6 +594,81 @@ def roofline_of(w, ms, steps, launches, peak, peak_kind):
     return roofline
 
 
+_PLACEMENT = None
+
+
+def host_placement(torch):
+    """The NUMA nodes this process may run on and the GPU's node (from the
+    PCI function's sysfs entry; None where the system does not say).  Where
+    there is more than one node, pinned buffers are allocated from a thread
+    bound to the CPUs of the GPU's node, so that their pages sit next to the
+    GPU's host link."""
+    global _PLACEMENT
+    if _PLACEMENT is None:
+        allowed = os.sched_getaffinity(0)
+        nodes = {}
+        base = "/sys/devices/system/node"
+        for name in (os.listdir(base) if os.path.isdir(base) else []):
+            if not (name.startswith("node") and name[4:].isdigit()):
+                continue
+            try:
+                with open(os.path.join(base, name, "cpulist")) as f:
+                    text = f.read().strip()
+            except OSError:
+                continue
+            cpus = set()
+            for part in filter(None, text.split(",")):
+                a, _, b = part.partition("-")
+                cpus.update(range(int(a), int(b or a) + 1))
+            if cpus & allowed:
+                nodes[int(name[4:])] = sorted(cpus & allowed)
+        gpu = None
+        try:
+            p = torch.cuda.get_device_properties(torch.cuda.current_device())
+            with open("/sys/bus/pci/devices/%04x:%02x:%02x.0/numa_node" % (p.pci_domain_id, p.pci_bus_id,
+                                                                          p.pci_device_id)) as f:
+                gpu = int(f.read().strip())
+        except Exception:           # no device properties or no sysfs entry: unknown
+            gpu = None
+        cpus = nodes.get(gpu) if gpu is not None and len(nodes) > 1 else None
+        _PLACEMENT = {"numa_nodes": len(nodes), "gpu_node": gpu, "bound_to_gpu_node": cpus is not None,
+                      "cpus": cpus}
+    return _PLACEMENT
+
+
+def pinned(torch, nbytes):
+    """Page-locked host memory of nbytes (a numpy uint8 array that keeps the
+    torch tensor alive), placed as host_placement says."""
+    cpus = host_placement(torch)["cpus"]
+    old = os.sched_getaffinity(0) if cpus else None
+    if cpus:
+        os.sched_setaffinity(0, cpus)
+    try:
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+    finally:
+        if old is not None:
+            os.sched_setaffinity(0, old)
+
+
+def host_link_gbs(torch, hin, hout):
+    """One copy of the run's own host buffers each way, after its timed
+    runs: what the host link gave these buffers (GB/s)."""
+    a = torch.from_numpy(hin.reshape(-1).view(np.uint8))
+    b = torch.from_numpy(hout.reshape(-1).view(np.uint8))
+    d = torch.empty(a.numel(), dtype=torch.uint8, device="cuda")
+    d.copy_(a, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d.copy_(a, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    b.copy_(d[:b.numel()], non_blocking=True)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    del d
+    return {"h2d": round(a.numel() / (t1 - t0) / 1e9, 1), "d2h": round(b.numel() / (t2 - t1) / 1e9, 1)}
+
+
 def e2e_of(w, torch, runs, dist=None, world=1):
     """The workload's run through the C ABI with host buffers: upload from
     pinned memory, run_steps time steps, download - averaged over runs."""
@@ -607,10 +682,13 @@ def e2e_of(w, torch, runs, dist=None, world=1):
     t1 = time.perf_counter()
     barrier(dist)
     e2e_s = max_over_ranks(dist, t1 - t0)
+    pl = host_placement(torch)
     return {"value": round(w.units * w.run_steps * runs * world / e2e_s / 1e9, 3), "unit": w.unit,
             "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
             "step": "upload from pinned host + %d time steps + download, through the C ABI" % w.run_steps,
-            "ms_per_step": round(e2e_s * 1e3 / runs, 3)}
+            "ms_per_step": round(e2e_s * 1e3 / runs, 3),
+            "host_link_gbs": host_link_gbs(torch, hin, hout),
+            "host_numa": {k: pl[k] for k in ("numa_nodes", "gpu_node", "bound_to_gpu_node")}}
 
 
 def measure(torch, w, steps, warmup, local, dist, world, peak, peak_kind):

@@ -71,3 +71,19 @@ def test_traffic_summaries_name_committed_profiles():
     for key, value, summary in rows:
         assert float(value) > 0
         assert os.path.exists(os.path.join(ROOT, "profiles", summary)), summary
+
+
+def test_host_placement_without_a_gpu_node_binds_nothing():
+    class NoDevice:
+        class cuda:
+            @staticmethod
+            def current_device():
+                raise RuntimeError("no GPU")
+
+    bench._PLACEMENT = None
+    try:
+        pl = bench.host_placement(NoDevice)
+        assert pl["gpu_node"] is None and pl["bound_to_gpu_node"] is False and pl["cpus"] is None
+        assert pl["numa_nodes"] >= 0
+    finally:
+        bench._PLACEMENT = None
