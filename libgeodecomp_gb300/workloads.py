@@ -10,7 +10,8 @@ numbers as this module, and large grids can be generated on the GPU.
 Logical cell order is x-fastest everywhere: ``idx = (z * ny + y) * nx + x``.
 
 The reference ships no dataset for this path; these generators stand in for
-the configurations the survey names (shapes, sizes and value distributions).
+the benchmark configurations' inputs (their shapes, sizes and value
+distributions).
 """
 from __future__ import annotations
 
