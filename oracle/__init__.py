@@ -3,8 +3,8 @@
 ``oracle/lgd_oracle.c`` restates the reference's algorithms in plain C;
 this module builds it into ``oracle/liblgd_oracle.so`` and exposes numpy
 wrappers.  Only the tests, the smoke check and the CPU-baseline leg of the
-benchmark may import it - as the checker, never as the thing measured or
-shipped.  ``oracle/_ref/lgd_ref`` (built by ``oracle/Makefile`` from the
+benchmark may import it - to compare results against, never as the thing
+measured or shipped.  ``oracle/_ref/lgd_ref`` (built by ``oracle/Makefile`` from the
 reference's own headers, only where they are present) is the reference
 itself; ``tests/golden/gen_golden.py`` runs it to pin this oracle.
 """

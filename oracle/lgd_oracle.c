@@ -1,8 +1,8 @@
 /*
  * CPU oracle: plain C restatement of the reference's algorithms for the
  * cell-update hot path.  TEST INFRASTRUCTURE ONLY - tests/, the smoke check
- * and bench.py's CPU-baseline leg call it as the checker; no product code
- * path links or calls it.
+ * and bench.py's CPU-baseline leg call it to compare results against; no
+ * product code path links or calls it.
  *
  * Pinned against golden fixtures written by running the reference's own
  * SerialSimulator (oracle/_ref/lgd_ref, built from the reference headers by
