@@ -163,12 +163,15 @@ class SurrogateNet:
 
 class PlainStencil:
     """The plain var-coef stencil (LGD_CELL_VARCOEF_F32 on a torus) working
-    on torch CUDA tensors: copy in, step, copy out."""
+    on torch CUDA tensors: copy in, step, copy out.  n: the edge of a cube,
+    or shape: (nz, ny, nx) of any torus."""
 
-    def __init__(self, n: int, precision: int = 4):
-        self.n = n
+    def __init__(self, n: int = 0, precision: int = 4, shape=None):
+        self.shape = tuple(shape) if shape is not None else (n, n, n)
+        self.n = self.shape[-1]
+        self.cells = int(np.prod(self.shape))
         self.cell = lgd.CELL_VARCOEF_F32 if precision == 4 else lgd.CELL_VARCOEF_F64
-        self.g = lgd.Grid(self.cell, (n, n, n), periodic=7)
+        self.g = lgd.Grid(self.cell, self.shape, periodic=7)
         self.elem = precision
 
     def close(self):
@@ -180,7 +183,8 @@ class PlainStencil:
         self._call("lgd_gpu_upload_device", 1, 0, kappa)
 
     def run(self, u, steps: int):
-        """u (torch CUDA tensor, n^3) <- u after steps plain steps."""
+        """u (torch CUDA tensor of the torus' shape) <- u after steps plain
+        steps."""
         import torch
         torch.cuda.synchronize()
         self._call("lgd_gpu_upload_device", 0, 0, u)
@@ -188,7 +192,7 @@ class PlainStencil:
         self._call("lgd_gpu_download_device", 0, 0, u)
 
     def _call(self, name, member, which, t):
-        assert t.is_contiguous() and t.numel() == self.n ** 3 and t.element_size() == self.elem
+        assert t.is_contiguous() and t.numel() == self.cells and t.element_size() == self.elem
         fn = getattr(lgd.lib(), name)
         fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
         fn.restype = ctypes.c_int
@@ -348,9 +352,11 @@ def run_surrogate_with_judge(params, u0, kappa, steps: int, tol: float = 1e-4, c
         t0 = time.perf_counter()
         for _ in range(steps // seg_steps):
             seg_start.copy_(u)
+            torch.cuda.synchronize()     # the copy (torch's stream) before the net's stream writes u
             net.advance(u, kappa, CALLS_PER_JUDGE - 1)
             net.synchronize()
             prev.copy_(u)
+            torch.cuda.synchronize()
             net.advance(u, kappa, 1)
             net.synchronize()
             check.copy_(prev)
