@@ -21,6 +21,7 @@
 #include <cuda.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "lgd_internal.h"
 #include "k_cells.cuh"
@@ -464,6 +465,30 @@ static int pick_zchunk(long long xy, int nz, long long resident)
     return best_chunk;
 }
 
+// Planes per CTA for a kernel bound by its arithmetic pipe (the IEEE FP64
+// cell: the FP64 pipe, not HBM): the split whose CTAs fill whole waves of
+// resident CTAs best, modelled time = waves x planes per CTA, chunks of at
+// least 8 planes.  A partial last wave leaves SMs idle while the others
+// finish, which an arithmetic-bound kernel pays in full (512^3: 10 chunks
+// of 52 planes make 4.2 waves, 19 chunks of 27 make 8.0).
+static int pick_zchunk_compute(long long xy, int nz, long long resident)
+{
+    int best_chunk = nz;
+    double best = 1e300;
+    const int max_split = std::max(1, nz / 8);
+    for (int split = 1; split <= max_split; ++split) {
+        const int chunk = (nz + split - 1) / split;
+        const int s = (nz + chunk - 1) / chunk;
+        const long long waves = (xy * s + resident - 1) / resident;
+        const double t = (double)waves * chunk;
+        if (t < best * 0.999) {
+            best = t;
+            best_chunk = chunk;
+        }
+    }
+    return best_chunk;
+}
+
 // resident CTAs of a kernel on the whole device
 static long long resident_ctas(const void *fn, int threads, int smem)
 {
@@ -505,23 +530,29 @@ static void launch_tma_typed(Grid& g, CUtensorMapDataType dt)
         g.tmap_base[src] = g.m[0].buf[src];
     }
     const int smem = tmak::S * tmak::Box<T>::SLOT;
-    static PerDevice<bool> setup;
-    setup.get([smem] {
+    static PerDevice<long long> setup;
+    const long long resident = setup.get([smem] {
         LGD_CHECK_CUDA(cudaFuncSetAttribute(tmak::jacobi7_tma_kernel<CELL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             smem));
-        return true;
+        return tmak::resident_ctas((const void *)tmak::jacobi7_tma_kernel<CELL>, tmak::THREADS, smem);
     });
     const int bx = (g.desc.nx + tmak::TX - 1) / tmak::TX;
     const int by = (g.desc.ny + tmak::TY - 1) / tmak::TY;
     const long long xy = (long long)bx * by;
-    // about 16 CTAs per SM over the launch (several waves of three resident
-    // ones): at 94% of HBM bandwidth the kernel is bound by DRAM, not by
-    // the copies a CTA has in flight, and short z chunks keep the tail of
-    // the launch short (measured: 400 GLUPS at 512^3 against 387 with the
-    // wave-count model the var-coef kernel uses)
-    int zsplit = (int)((152LL * 16 + xy - 1) / xy);
-    zsplit = std::max(1, std::min(zsplit, (g.desc.nz + 15) / 16));
-    int zchunk = (g.desc.nz + zsplit - 1) / zsplit;
+    int zchunk, zsplit;
+    if (std::is_same<CELL, Jacobi7F64>::value) {
+        // bound by the FP64 pipe: whole waves
+        zchunk = tmak::pick_zchunk_compute(xy, g.desc.nz, resident);
+    } else {
+        // about 16 CTAs per SM over the launch (several waves of three
+        // resident ones): at 94% of HBM bandwidth the kernel is bound by
+        // DRAM, not by the copies a CTA has in flight, and short z chunks
+        // keep the tail of the launch short (measured: 400 GLUPS at 512^3
+        // against 387 with the wave-count model the var-coef kernel uses)
+        zsplit = (int)((152LL * 16 + xy - 1) / xy);
+        zsplit = std::max(1, std::min(zsplit, (g.desc.nz + 15) / 16));
+        zchunk = (g.desc.nz + zsplit - 1) / zsplit;
+    }
     zsplit = (g.desc.nz + zchunk - 1) / zchunk;
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(g.tmap[src]);
     tmak::jacobi7_tma_kernel<CELL><<<dim3(bx, by, zsplit), tmak::THREADS, smem, g.stream>>>(
