@@ -211,7 +211,8 @@ class SlabSurrogate:
             left -= LAYERS
             self.net.synchronize()
             check.copy_(prev)
-            assert prev_left >= STEPS_PER_CALL
+            if prev_left < STEPS_PER_CALL:           # _need above makes this impossible
+                raise RuntimeError("the judge's state holds too few exact ghost planes")
             self.plain.run(check, STEPS_PER_CALL)
             err = self._rel_l2(u, check)
             self.stats["judge_errors"].append(err)
