@@ -922,6 +922,42 @@ def timed_on_stream(torch, stream_ptr, fn):
     return a.elapsed_time(b), time.perf_counter() - t0
 
 
+def rank_e2e(torch, one_run, hin, hout, units, run_steps, runs, dist, world, unit="GLUPS"):
+    """End to end over ranks: every rank runs one_run() - its upload from
+    pinned host memory, run_steps steps with their exchanges, its download -
+    runs times after one warm-up; the max over ranks of the host time."""
+    one_run()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(max(1, runs)):
+        one_run()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    barrier(dist)
+    runs = max(1, runs)
+    return {"value": round(units * world * run_steps * runs / e2e_s / 1e9, 3), "unit": unit,
+            "h2d_bytes_per_step": int(hin.nbytes), "d2h_bytes_per_step": int(hout.nbytes),
+            "step": "per rank: upload from pinned host + %d time steps with exchanges + download, through the "
+                    "library's API" % run_steps, "ms_per_step": round(e2e_s * 1e3 / runs, 3)}
+
+
+def slab_e2e(torch, s, run_steps, runs, dist, world, units):
+    """rank_e2e of a slab grid: each rank's local planes (ghost planes
+    included) in and out."""
+    dt = np.dtype(s.grid.members[0])
+    nbytes = int(np.prod(s.local_shape)) * dt.itemsize
+    hin = pinned(torch, nbytes).view(dt).reshape(s.local_shape)
+    hout = pinned(torch, nbytes).view(dt).reshape(s.local_shape)
+    s.grid.download(0, out=hin)
+
+    def one_run():
+        s.grid.upload(0, hin)
+        s.since = s.period             # ghost planes refreshed before the first step
+        s.step(run_steps)
+        s.grid.download(0, out=hout)
+    return rank_e2e(torch, one_run, hin, hout, units, run_steps, runs, dist, world)
+
+
 def run_slabs(args, world, rank, local, dist, peak, peak_kind):
     """Weak scaling over z-slabs: every rank owns a size^3 slab of the
     size x size x (size * world) grid and exchanges ghost planes with its
@@ -963,6 +999,13 @@ def run_slabs(args, world, rank, local, dist, peak, peak_kind):
     units = n * n if args.workload == "gol_u8_8192" else n * n * n
     value = units * world * args.steps / dt / 1e9
     launches = s.launch_count()
+    e2e = None
+    if not args.no_e2e:
+        run_steps = {"gol_u8_8192": GoLWorkload.run_steps}.get(args.workload, JacobiWorkload.run_steps)
+        try:
+            e2e = slab_e2e(torch, s, run_steps, args.e2e_runs, dist, world, units)
+        except Exception as e:      # the device-timed line stands without it
+            e2e = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0:
         line = {"metric": JACOBI_METRIC if args.workload.startswith("jacobi7") else METRICS[args.workload],
                 "value": round(value, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
@@ -972,7 +1015,7 @@ def run_slabs(args, world, rank, local, dist, peak, peak_kind):
                 "config": workload_config(args.workload, args, world), "gpu_launches": launches,
                 "timing": "CUDA events on each rank's grid stream around its steps (ghost exchanges included), "
                           "max over ranks", "host_ms_per_step": round(host_s * 1e3 / args.steps, 4),
-                "slabs": s.describe(), "e2e": None, "cpu_baseline": None, "clocks": clk.summary()}
+                "slabs": s.describe(), "e2e": e2e, "cpu_baseline": None, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     s.close()
     dist.destroy_process_group()
@@ -999,6 +1042,20 @@ def run_sell_shards(args, world, rank, local, dist):
     barrier(dist)
     dt = max_over_ranks(dist, ms * 1e-3)
     host_s = max_over_ranks(dist, host_s)
+    e2e = None
+    if not args.no_e2e:
+        try:
+            hin = pinned(torch, n * 8).view(np.float64)
+            hout = pinned(torch, n * 8).view(np.float64)
+            hin[:] = workloads.sell_values(n, seed=42)
+
+            def one_run():
+                g.upload(hin)
+                s.step(SellWorkload.run_steps)
+                g.download(out=hout)
+            e2e = rank_e2e(torch, one_run, hin, hout, n, SellWorkload.run_steps, args.e2e_runs, dist, 1)
+        except Exception as e:      # the device-timed line stands without it
+            e2e = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0:
         line = {"metric": METRICS["sell_f64_4m"], "value": round(n * args.steps / dt / 1e9, 3), "unit": "GLUPS",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -1008,7 +1065,7 @@ def run_sell_shards(args, world, rank, local, dist):
                 "config": workload_config("sell_f64_4m", args, world), "gpu_launches": args.steps,
                 "timing": "CUDA events on each rank's grid stream around its steps (all-gathers included), "
                           "max over ranks", "host_ms_per_step": round(host_s * 1e3 / args.steps, 4),
-                "row_blocks": s.describe(), "e2e": None, "cpu_baseline": None, "clocks": clk.summary()}
+                "row_blocks": s.describe(), "e2e": e2e, "cpu_baseline": None, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     g.close()
     dist.destroy_process_group()
