@@ -20,7 +20,7 @@ import time
 
 import numpy as np
 
-from . import lgd, workloads
+from . import lgd
 
 STEPS_PER_CALL = 16
 CALLS_PER_JUDGE = 8

@@ -3,7 +3,6 @@ gloo processes, with stand-ins for the network (four 3^3 layers per call,
 each reaching one plane further along z) and the plain stencil (one plane
 per step), give the single torus' result bit for bit, with the judge's
 fallback taken and not taken; the ghost zone must hold one judge run."""
-import json
 import os
 import socket
 import subprocess
