@@ -1,17 +1,18 @@
 """The multi-process side of bench.py on CPU ranks (gloo, world size 2).
 
-With --gpus N > 1 every rank advances its own replica (no collective on
-the data path); the only cross-rank work is the barrier around the timed
-region and the maximum of the ranks' times, which these tests run on two
-gloo ranks.  The reference arm under torchrun prints one line from rank 0
-and lets the other ranks exit without work."""
+With --gpus N > 1 the structured workloads run as slabs with ghost-plane
+exchanges, SELL as row blocks with an all-gather and the ensemble as one
+ensemble per rank (their exchanges are covered by tests/test_slabs.py and
+tests/test_sell_shards.py); what every line shares is the barrier around
+the timed region and the maximum of the ranks' times, which these tests
+run on two gloo ranks.  The reference arm under torchrun prints one line
+from rank 0 and lets the other ranks exit without work."""
 import json
 import os
 import socket
 import subprocess
 import sys
 
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
