@@ -41,10 +41,13 @@ this machine), OpenMP over all cores, on whole time steps of the same input,
 with the same config block as the GPU arm.
 
 Under torchrun (--gpus N > 1) the structured workloads are decomposed into
-z-slabs, one per rank (weak scaling: every rank owns a 512^3 slab of a
-512 x 512 x 512N grid), with a ghost-zone exchange of R*T planes every T
-steps (libgeodecomp_gb300.slabs); rank 0 prints the line with the max time
-over ranks.  Other workloads run one replica per rank.
+slabs, one per rank (weak scaling: every rank owns a 512^3 slab of a
+512 x 512 x 512N grid, Game of Life 8192^2 cells of a y-cut torus), with a
+ghost-zone exchange of R*T planes every T steps (libgeodecomp_gb300.slabs);
+SELL-C-sigma runs its 4,194,304 nodes over row blocks with an all-gather
+per step (strong scaling, libgeodecomp_gb300.sell_shards), the ensemble
+one 512-cavity ensemble per rank; rank 0 prints the line with the max time
+over ranks.
 """
 from __future__ import annotations
 
