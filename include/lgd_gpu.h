@@ -70,8 +70,9 @@ int lgd_gpu_device_count(int *count);
  *                          pass of two steps sums both exactly and rounds
  *                          once (within one unit of two single steps).  e is
  *                          raised when an upload needs it and lowered (an
- *                          exact shift) after every upload and every 256
- *                          steps when the grid's values have shrunk, so a
+ *                          exact shift) when the grid's values have shrunk,
+ *                          checked after an upload whose maximum lies below
+ *                          e's range and every 256 steps, so a
  *                          decaying grid keeps 57 significant bits at its
  *                          maximum; such a check waits for the device.  For
  *                          GPUs whose FP64 pipe, not memory, would bound the
@@ -238,7 +239,7 @@ int lgd_gpu_fixed_point_exponent(lgd_handle *h, int *exp);
  * both buffers are rescaled, exactly when e falls (a shift left; values
  * that would not fit return LGD_ERR_RANGE and leave the grid unchanged),
  * rounded to nearest when it rises.  pin != 0 keeps e from now on: the
- * checks after uploads and every 256 steps no longer lower it (an upload
+ * checks after an upload and every 256 steps no longer lower it (an upload
  * whose values need more still raises it).  For grids that exchange raw
  * planes (a z-slab decomposition, lgd_gpu_copy_planes), which need one
  * exponent on every rank. */
