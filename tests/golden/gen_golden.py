@@ -11,7 +11,7 @@ FFT, whose last bits may vary by platform), so a drifting generator is
 caught instead of silently changing what the fixture means.
 
 Run in the build container (the reference is not present elsewhere):
-    python tests/golden/gen_golden.py
+    python tests/golden/gen_golden.py [--only edge_shapes]
 """
 from __future__ import annotations
 
@@ -213,7 +213,66 @@ def varcoef(tmp, name, n, steps, length):
                         length=np.array(length), u0=u0, k=k, out=out)
 
 
+# degenerate and odd shapes of every cell, all in edge_shapes.npz
+EDGE_JACOBI = [("cube", 1, 1, 9), ("cube", 9, 1, 1), ("cube", 1, 7, 1), ("cube", 2, 3, 5), ("cube", 5, 1, 3),
+               ("torus", 1, 3, 4), ("torus", 4, 1, 1), ("torus", 3, 4, 1), ("torus", 1, 2, 2)]
+# (the reference refuses a 3D torus with y = 1 and z > 1: "expected 1D grid, but z != 1")
+EDGE_GOL = [(7, 5), (1, 9), (9, 1), (33, 17), (2, 2)]
+EDGE_LBM = [2, 3]
+EDGE_VARCOEF = [(1, 1, 4), (3, 5, 2), (7, 3, 5)]
+EDGE_SELL = [(1000, 32, 256), (100, 4, 60), (130, 8, 16), (70, 2, 4)]      # (n, C, sigma)
+EDGE_STEPS = 6
+
+
+def edge_key(kind, *dims):
+    return "%s_%s" % (kind, "x".join(str(d) for d in dims))
+
+
+def edge_shapes(tmp):
+    """Degenerate and odd shapes (axes of extent 1 and 2, sizes that are
+    not multiples of C or sigma, boxes that are all wall cells) for every
+    cell, EDGE_STEPS steps each, from seeded inputs (seed 7)."""
+    out = {}
+    for topo, nx, ny, nz in EDGE_JACOBI:
+        u0 = workloads.jacobi_initial(nx, ny, nz, seed=7)
+        u0.tofile(os.path.join(tmp, "in.f64"))
+        run(["jacobi7", topo, nx, ny, nz, EDGE_STEPS, "in.f64", "out.f64", "serial"], tmp)
+        out[edge_key("jacobi_" + topo, nx, ny, nz)] = np.fromfile(os.path.join(tmp, "out.f64"),
+                                                                  dtype=np.float64).reshape(nz, ny, nx)
+    for nx, ny in EDGE_GOL:
+        c0 = workloads.gol_initial(nx, ny, seed=7)
+        c0.tofile(os.path.join(tmp, "in.u8"))
+        run(["gol", nx, ny, EDGE_STEPS, "in.u8", "out.u8", "serial"], tmp)
+        out[edge_key("gol", nx, ny)] = np.fromfile(os.path.join(tmp, "out.u8"), dtype=np.uint8).reshape(ny, nx)
+    for L in EDGE_LBM:
+        run(["lbm", L, EDGE_STEPS, repr(1.5), repr(0.05), "out.f64", "serial"], tmp)
+        out[edge_key("lbm", L)] = np.fromfile(os.path.join(tmp, "out.f64"), dtype=np.float64).reshape(19, L, L, L)
+    for nx, ny, nz in EDGE_VARCOEF:
+        n = nx * ny * nz
+        u0 = workloads.uniform(7, workloads.STREAM_GRID, n).reshape(nz, ny, nx)
+        k = 0.02 + 0.13 * workloads.uniform(7, workloads.STREAM_DEGREE, n).reshape(nz, ny, nx)
+        u0.tofile(os.path.join(tmp, "u.f64"))
+        k.tofile(os.path.join(tmp, "k.f64"))
+        run(["varcoef", nx, ny, nz, EDGE_STEPS, "u.f64", "k.f64", "out.f64", "serial"], tmp)
+        out[edge_key("varcoef", nx, ny, nz)] = np.fromfile(os.path.join(tmp, "out.f64"),
+                                                           dtype=np.float64).reshape(nz, ny, nx)
+    for n, C, sigma in EDGE_SELL:
+        rp, col, w = workloads.powerlaw_graph(n, seed=7)
+        x0 = workloads.sell_values(n, seed=7)
+        write_csr(tmp, rp, col, w)
+        x0.tofile(os.path.join(tmp, "x.f64"))
+        run(["sell", C, sigma, n, len(col), EDGE_STEPS, "rp.i64", "col.i32", "w.f64", "x.f64", "out.f64", "serial"],
+            tmp)
+        out[edge_key("sell", n, C, sigma)] = np.fromfile(os.path.join(tmp, "out.f64"), dtype=np.float64)
+    np.savez_compressed(os.path.join(OUT, "edge_shapes.npz"), steps=np.array(EDGE_STEPS), seed=np.array(7), **out)
+
+
 def main():
+    if sys.argv[1:] == ["--only", "edge_shapes"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            edge_shapes(tmp)
+        print("edge_shapes.npz written to", OUT)
+        return
     with tempfile.TemporaryDirectory() as tmp:
         jacobi(tmp, "jacobi7_cube_24x20x16", "cube", 24, 20, 16, 10)
         jacobi(tmp, "jacobi7_torus_17x13x11", "torus", 17, 13, 11, 7)
@@ -227,6 +286,7 @@ def main():
         lbm(tmp, "lbm_L24", 24, 100, 1.2, 0.05, full=False)
         varcoef(tmp, "varcoef_16", 16, 20, 4.0)
         bov(tmp, "bov_jacobi_24x20x16", 24, 20, 16, 6)
+        edge_shapes(tmp)
     print("fixtures written to", OUT)
 
 

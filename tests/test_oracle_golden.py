@@ -166,3 +166,41 @@ def test_bov_fixture_matches_oracle_and_format():
         header = bytes(g["bov_%d" % step]).decode()
         assert header.startswith("TIME: %d\nDATA_FILE: jac.%05d.data\nDATA_SIZE: %d %d %d\n" % (step, step, nx, ny, nz))
         assert "DATA_FORMAT: DOUBLE\nVARIABLE: temp\n" in header
+
+
+def _edge_cases():
+    g = load("edge_shapes")
+    return sorted(k for k in g.files if k not in ("steps", "seed"))
+
+
+@pytest.mark.parametrize("key", _edge_cases())
+def test_edge_shapes_bit_exact(key):
+    """Degenerate and odd shapes - axes of extent 1 and 2, boxes that are
+    all wall cells, node counts that are not multiples of C or sigma - as
+    the reference computes them (tests/golden/gen_golden.py edge_shapes)."""
+    g = load("edge_shapes")
+    steps, seed = int(g["steps"]), int(g["seed"])
+    kind, dims = key.rsplit("_", 1)
+    dims = [int(d) for d in dims.split("x")]
+    want = g[key]
+    if kind in ("jacobi_cube", "jacobi_torus"):
+        nx, ny, nz = dims
+        got = oracle.jacobi7(workloads.jacobi_initial(nx, ny, nz, seed=seed), steps, torus=kind == "jacobi_torus")
+    elif kind == "gol":
+        nx, ny = dims
+        got = oracle.gol(workloads.gol_initial(nx, ny, seed=seed), steps)
+    elif kind == "lbm":
+        got = oracle.lbm(dims[0], steps, 1.5, 0.05)
+    elif kind == "varcoef":
+        nx, ny, nz = dims
+        n = nx * ny * nz
+        u0 = workloads.uniform(seed, workloads.STREAM_GRID, n).reshape(nz, ny, nx)
+        k = 0.02 + 0.13 * workloads.uniform(seed, workloads.STREAM_DEGREE, n).reshape(nz, ny, nx)
+        got = oracle.varcoef(u0, k, steps)
+    elif kind == "sell":
+        n, C, sigma = dims
+        got = _sell_run(n, C, sigma, steps, seed)[2]
+    else:
+        raise AssertionError("unknown fixture " + key)
+    assert got.shape == want.shape
+    np.testing.assert_array_equal(got, want)
