@@ -600,7 +600,7 @@ def roofline_of(w, ms, steps, launches, peak, peak_kind):
 _PLACEMENT = None
 
 
-def host_placement(torch):
+def host_placement(torch, sysfs: str = "/sys"):
     """The NUMA nodes this process may run on and the GPU's node (from the
     PCI function's sysfs entry; None where the system does not say).  Where
     there is more than one node, pinned buffers are allocated from a thread
@@ -610,7 +610,7 @@ def host_placement(torch):
     if _PLACEMENT is None:
         allowed = os.sched_getaffinity(0)
         nodes = {}
-        base = "/sys/devices/system/node"
+        base = os.path.join(sysfs, "devices", "system", "node")
         for name in (os.listdir(base) if os.path.isdir(base) else []):
             if not (name.startswith("node") and name[4:].isdigit()):
                 continue
@@ -628,8 +628,8 @@ def host_placement(torch):
         gpu = None
         try:
             p = torch.cuda.get_device_properties(torch.cuda.current_device())
-            with open("/sys/bus/pci/devices/%04x:%02x:%02x.0/numa_node" % (p.pci_domain_id, p.pci_bus_id,
-                                                                          p.pci_device_id)) as f:
+            with open(os.path.join(sysfs, "bus", "pci", "devices", "%04x:%02x:%02x.0" % (
+                    p.pci_domain_id, p.pci_bus_id, p.pci_device_id), "numa_node")) as f:
                 gpu = int(f.read().strip())
         except Exception:           # no device properties or no sysfs entry: unknown
             gpu = None

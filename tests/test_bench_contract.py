@@ -87,3 +87,41 @@ def test_host_placement_without_a_gpu_node_binds_nothing():
         assert pl["numa_nodes"] >= 0
     finally:
         bench._PLACEMENT = None
+
+
+def test_host_placement_binds_to_the_gpu_node(tmp_path):
+    """Two NUMA nodes that share this process's CPUs, the GPU's PCI
+    function on the second: pinned buffers are allocated from that node's
+    CPUs."""
+    allowed = sorted(os.sched_getaffinity(0))
+    if len(allowed) < 2:
+        pytest.skip("needs two CPUs")
+    half = len(allowed) // 2
+    for i, cpus in enumerate((allowed[:half], allowed[half:])):
+        d = tmp_path / "devices" / "system" / "node" / ("node%d" % i)
+        d.mkdir(parents=True)
+        (d / "cpulist").write_text(",".join(str(c) for c in cpus) + "\n")
+    pci = tmp_path / "bus" / "pci" / "devices" / "0000:00:07.0"
+    pci.mkdir(parents=True)
+    (pci / "numa_node").write_text("1\n")
+
+    class Props:
+        pci_domain_id, pci_bus_id, pci_device_id = 0, 0, 7
+
+    class FakeTorch:
+        class cuda:
+            @staticmethod
+            def current_device():
+                return 0
+
+            @staticmethod
+            def get_device_properties(dev):
+                return Props()
+
+    bench._PLACEMENT = None
+    try:
+        pl = bench.host_placement(FakeTorch, sysfs=str(tmp_path))
+        assert pl["numa_nodes"] == 2 and pl["gpu_node"] == 1 and pl["bound_to_gpu_node"]
+        assert pl["cpus"] == allowed[half:]
+    finally:
+        bench._PLACEMENT = None
